@@ -1,0 +1,161 @@
+/*
+ * mcgpu.h -- C ABI of the GB300 fixed-source particle-history library.
+ *
+ * Drop-in for the fixed-source path of MC-old's Simulator (C++, in-process):
+ * each entry point names the reference interface it replaces.  Plain C types
+ * only: no C++ or framework types cross this boundary.
+ *
+ * Conventions
+ *  - Every call returns an mc_status; nothing exits or throws across the ABI
+ *    (the reference calls std::exit or a bare throw, setup.cpp:235,579;
+ *    general.cpp:33).  mc_last_error() gives the message of the last failure
+ *    on a handle.
+ *  - The library owns device memory; the caller owns every output buffer.
+ *  - One mc_problem per host thread.  Calls on one handle are not re-entrant.
+ *    Each handle has its own CUDA stream.
+ *  - Results are deterministic for a given (seed, history range, mode).
+ *  - Histories are keyed into a counter-based Philox4x32-10 stream by
+ *    (seed, history, particle, event, draw), so any history range can be run
+ *    separately and merged ("resume" = run [a, b) then [b, c)).
+ */
+#ifndef MCGPU_H
+#define MCGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mc_problem mc_problem;
+
+typedef enum {
+    MC_OK = 0,
+    MC_ERR_INPUT = 1,     /* malformed or unsupported input.xml / tables */
+    MC_ERR_CUDA = 2,      /* CUDA runtime error (no device, launch failure) */
+    MC_ERR_OVERFLOW = 3,  /* particle bank or split stack capacity exceeded */
+    MC_ERR_LOST = 4,      /* a particle left every cell (general.cpp:31-33) */
+    MC_ERR_TIMEOUT = 5,   /* a bounded device-side wait ran out */
+    MC_ERR_NAN = 6,       /* non-finite particle weight or position */
+    MC_ERR_NOMEM = 7,     /* host or device allocation failed */
+    MC_ERR_ARG = 8        /* bad argument (null pointer, index out of range) */
+} mc_status;
+
+typedef enum {
+    /* FP64 history-based, the reference's arithmetic order, portable
+     * elementary functions, tallies folded in history order: every history's
+     * event sequence and every tally bin equal the CPU oracle's bit for bit. */
+    MC_FP64_REPLAY = 0,
+    /* FP64 history-based with the GPU's native FP64 libm and a tree fold:
+     * the plain double-precision GPU history path. */
+    MC_FP64_PLAIN = 1,
+    /* FP32 tracking, event-based kernels over a structure-of-arrays bank with
+     * ballot/prefix-sum compacted event queues, FP64 tally accumulation. */
+    MC_MIXED_EVENT = 2
+} mc_mode;
+
+/* Launch / capacity knobs.  Pass NULL to mc_run for the defaults (or the
+ * values picked by mc_autotune). */
+typedef struct {
+    uint32_t block;          /* threads per block (0 = default) */
+    uint32_t grid_blocks;    /* blocks, 0 = fill the GPU */
+    uint32_t stack_depth;    /* FP64 modes: split-particle stack per thread */
+    uint32_t chunk;          /* FP64 modes: histories per fold chunk (0 = auto) */
+    uint32_t bank_capacity;  /* event mode: particles in flight (0 = auto) */
+    uint32_t record_digests; /* FP64 modes: keep per-history event digests */
+} mc_tune;
+
+/* Event counters and timing of the last mc_run.  The counts follow the
+ * reference's own bookkeeping: flights is its Ntrack (simulator.h:109,
+ * general.cpp:76). */
+typedef struct {
+    uint64_t flights;         /* move_particle calls */
+    uint64_t collisions;
+    uint64_t crossings;
+    uint64_t tally_updates;   /* per-history bin accumulations */
+    uint64_t particles;       /* particles walked, split copies included */
+    uint64_t splits;          /* copies made by importance splitting */
+    uint64_t xs_evals;        /* macroscopic cross-section evaluations */
+    uint64_t freegas_iters;   /* free-gas rejection-loop iterations */
+    uint64_t nuc_lookups;     /* sum over flights of the material's nuclide count */
+    uint64_t histories;       /* histories in the last run */
+    double   transport_ms;    /* device time of the transport kernels */
+    double   fold_ms;         /* device time of the history fold */
+    double   total_ms;        /* device time of the whole mc_run */
+    uint32_t launches;        /* kernels launched by the last mc_run */
+    uint32_t iterations;      /* event mode: event-loop iterations */
+} mc_counters;
+
+/* Replaces Simulator::Simulator(io_dir) (src/simulator/setup.cpp:30): reads
+ * <io_dir>/input.xml; ZAID tables come from <xs_dir>/<ZAID>.txt, where
+ * xs_dir NULL means "./xs_library" as in the reference (setup.cpp:326). */
+mc_status mc_problem_load_xml(const char *io_dir, const char *xs_dir, mc_problem **out);
+
+/* Copies the problem tables from the handle's pinned host copy to the device
+ * again (after the host copy changed, or to time a cold start).  The
+ * reference keeps its tables in host memory only; this has no counterpart
+ * there beyond the table construction in Simulator::Simulator. */
+mc_status mc_problem_upload(mc_problem *p);
+
+/* Bytes of the device copy of the problem tables (what mc_problem_upload
+ * moves host -> device). */
+mc_status mc_problem_table_bytes(const mc_problem *p, uint64_t *bytes);
+
+/* Releases a handle (the reference's Simulator destructor). */
+mc_status mc_problem_free(mc_problem *p);
+
+/* Replaces Simulator::start() (src/simulator/handler.cpp:11-48) for the
+ * histories [first_history, first_history + n_histories).  Tally sums
+ * accumulate across calls; call mc_reset_tallies to start over. */
+mc_status mc_run(mc_problem *p, uint64_t first_history, uint64_t n_histories, uint64_t seed,
+                 mc_mode mode, const mc_tune *tune);
+
+/* Zeroes the accumulated tally sums and the history count. */
+mc_status mc_reset_tallies(mc_problem *p);
+
+/* Number of estimators (the reference's Estimators.size(), simulator.h:122). */
+mc_status mc_tally_count(const mc_problem *p, uint32_t *n_estimators);
+
+/* Bins of estimator est (Estimator::tally_size, Estimator.cpp:429-432). */
+mc_status mc_tally_size(const mc_problem *p, uint32_t est, uint64_t *n_bins);
+
+/* Name of estimator est (the XML name attribute, setup.cpp:641-642). */
+mc_status mc_estimator_name(const mc_problem *p, uint32_t est, char *buf, size_t cap);
+
+/* Replaces Estimators[est]->tally(j).mean / .uncer (Estimator.cpp:347-367,
+ * 424-427): mean and standard error over the histories run so far, plus the
+ * raw per-bin sums of history totals and of their squares.  Any output
+ * pointer may be NULL; cap is the capacity of each non-NULL array. */
+mc_status mc_tally_read(const mc_problem *p, uint32_t est, double *mean, double *sigma,
+                        double *sum, double *sumsq, uint64_t cap);
+
+/* Counters of the last run (Ntrack plus the per-event counts). */
+mc_status mc_counters_read(const mc_problem *p, mc_counters *out);
+
+/* Per-history event digests of the last FP64 run made with
+ * tune->record_digests (n entries, one per history in run order). */
+mc_status mc_digests_read(const mc_problem *p, uint64_t *out, uint64_t cap);
+
+/* Histories requested in the input (<description samples>, setup.cpp:50). */
+mc_status mc_nsample(const mc_problem *p, uint64_t *nsample);
+
+/* Histories folded into the tallies so far. */
+mc_status mc_histories_run(const mc_problem *p, uint64_t *n);
+
+/* Replaces Simulator::report(io_dir) (src/simulator/report.cpp:9-50): writes
+ * the output.h5 group/dataset layout (/summary, one group per estimator with
+ * its filter grids and <score>/mean, <score>/uncertainty) as a JSON file at
+ * path, HDF5 not being available. */
+mc_status mc_report(const mc_problem *p, const char *path);
+
+/* Human-readable message for the last failing call on p (never NULL). */
+const char *mc_last_error(const mc_problem *p);
+
+/* Static name of a status code. */
+const char *mc_status_string(mc_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCGPU_H */

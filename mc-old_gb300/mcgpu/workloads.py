@@ -5,7 +5,11 @@ MC-old's Simulator, src/simulator/setup.cpp:30-1066) and, for
 continuous-energy problems, an ``xs_library/`` of 6-column tables
 (xs_library/README.txt:1-7: energy, sigma_s, sigma_c, sigma_f, nu, nu_d).
 Random parameters come from ``numpy.random.Generator(PCG64(1000 + k))`` where
-``k`` is the workload's number, so every writer is deterministic.
+``k`` is the workload's number.  Only uniform draws and IEEE arithmetic
+(+, -, *, /, sqrt) touch the written numbers; logarithms and exponentials go
+through Python's ``decimal`` module, which rounds correctly, so every writer
+produces the same bytes on every machine (libm and numpy's exp/log differ in
+the last bit between x86-64 and aarch64).
 
 Workloads (sizes are the defaults; all can be shrunk for tests):
   slab_1g            20 cm 1-group slab, sigma_t = 1, c = 0.5, inward
@@ -23,6 +27,7 @@ Workloads (sizes are the defaults; all can be shrunk for tests):
 """
 from __future__ import annotations
 
+import decimal
 import math
 import os
 
@@ -33,6 +38,30 @@ FMT = "%.17g"
 
 def _rng(k: int) -> np.random.Generator:
     return np.random.Generator(np.random.PCG64(1000 + k))
+
+
+def log_uniform_grid(lo: float, hi: float, n: int) -> np.ndarray:
+    """n points, log-uniform from lo to hi, each exp(ln lo + i*step) rounded
+    once from 40-digit decimal arithmetic (identical on every platform)."""
+    ctx = decimal.Context(prec=40)
+    a = ctx.ln(decimal.Decimal(repr(lo)))
+    b = ctx.ln(decimal.Decimal(repr(hi)))
+    step = ctx.divide(ctx.subtract(b, a), decimal.Decimal(n - 1))
+    out = np.empty(n)
+    for i in range(n):
+        out[i] = float(ctx.exp(ctx.add(a, ctx.multiply(step, decimal.Decimal(i)))))
+    out[0], out[-1] = lo, hi
+    return out
+
+
+def dirichlet1(rng: np.random.Generator, k: int) -> np.ndarray:
+    """Dirichlet(1, ..., 1) on k components as the spacings of k-1 sorted
+    uniforms (uniform on the simplex; needs no logarithm)."""
+    if k == 1:
+        return np.ones(1)
+    u = np.sort(rng.uniform(0.0, 1.0, size=k - 1))
+    edges = np.concatenate([[0.0], u, [1.0]])
+    return np.diff(edges)
 
 
 def write_xs_table(path: str, A: float, E, sig_s, sig_c) -> None:
@@ -119,8 +148,7 @@ def ce_tables(n_points: int = 20_000, k: int = 2):
     """Synthetic pointwise cross sections: sigma_s = s0/(1+E/Ec),
     sigma_c = c0*sqrt(0.0253/E) on a log-uniform grid 1e-5 eV .. 20 MeV."""
     rng = _rng(k)
-    E = np.exp(np.linspace(math.log(1e-5), math.log(2e7), n_points))
-    E[0], E[-1] = 1e-5, 2e7
+    E = log_uniform_grid(1e-5, 2e7, n_points)
     out = {}
     for name, zaid, A in CE_NUCLIDES:
         s0 = rng.uniform(2.0, 20.0)
@@ -189,7 +217,7 @@ def mg_slab_data(n_regions: int, G: int, k: int, c_lo=0.5, c_hi=0.95, st_lo=0.2,
         for g in range(G):
             c = rng.uniform(c_lo, c_hi)
             lo = g if downscatter_only else 0
-            frac = rng.dirichlet(np.ones(G - lo))
+            frac = dirichlet1(rng, G - lo)
             sca[r, g, lo:] = c * tot[r, g] * frac
     return tot, sca
 

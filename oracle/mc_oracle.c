@@ -363,14 +363,21 @@ static double macro_xs(orc_ctx *C, int m, int which, const orc_particle *p)
 
 typedef struct { int bin; double l; } orc_il;
 
-/* Filter::idx_l (Estimator.cpp:133-246); returns the number of (bin, l) pairs
- * written to out (cap entries). */
+/* (bin, length) pairs of all filters of one score call; a time filter that
+ * spans more bins than fit is reported as ORC_ERR_OVERFLOW (the GPU path has
+ * the same fixed budget). */
+#define ORC_MAX_FILT 8
+#define ORC_MAX_IL 64
+
+/* Filter::idx_l (Estimator.cpp:133-246); writes the pairs to out and returns
+ * their number, or -1 when more than cap would be needed. */
 static int filter_idx_l(const orc_problem *P, int f, const orc_particle *p, double l,
                         orc_il *out, int cap)
 {
     const double *grid = P->filt_grid + P->filt_grid_off[f];
     const int glen = P->filt_grid_len[f];
     const int nbin = glen - 1;
+    if (cap < 1) return -1;
     switch (P->filt_kind[f]) {
     case ORC_F_SURFACE: {
         int b = orc_binary_search((double)p->surf_old, grid, glen) + 1;
@@ -398,13 +405,15 @@ static int filter_idx_l(const orc_problem *P, int f, const orc_particle *p, doub
             return 0;
         }
         const int num_bin = loc2 - loc1 - 1;
-        if (loc1 >= 0 && n < cap) {
+        const int need = (loc1 >= 0) + (num_bin > 0 ? num_bin : 0) + (loc2 < nbin);
+        if (need > cap) return -1;
+        if (loc1 >= 0) {
             out[n].bin = loc1; out[n].l = (grid[loc1 + 1] - p->t_old) * p->speed; ++n;
         }
-        for (int i = 1; i <= num_bin && n < cap; ++i) {
+        for (int i = 1; i <= num_bin; ++i) {
             out[n].bin = loc1 + i; out[n].l = (grid[loc1 + i + 1] - grid[loc1 + i]) * p->speed; ++n;
         }
-        if (loc2 < nbin && n < cap) {
+        if (loc2 < nbin) {
             out[n].bin = loc2; out[n].l = (p->t - grid[loc2]) * p->speed; ++n;
         }
         return n;
@@ -432,9 +441,6 @@ static double score_value(orc_ctx *C, int sc, const orc_particle *p, double l)
     }
 }
 
-#define ORC_MAX_FILT 8
-#define ORC_MAX_IL 256
-
 /* Estimator::score (Estimator.cpp:298-336) */
 static void estimator_score(orc_ctx *C, int e, const orc_particle *p, double l_in)
 {
@@ -443,27 +449,34 @@ static void estimator_score(orc_ctx *C, int e, const orc_particle *p, double l_i
     const int s0 = P->est_score_off[e], ns = P->est_score_off[e + 1] - s0;
     const double *fac = P->est_factor + P->est_factor_off[e];
     double *hist = C->hist + P->est_bin_off[e];
-    static __thread orc_il il[ORC_MAX_FILT][ORC_MAX_IL];
-    int nil[ORC_MAX_FILT];
-    int idx[ORC_MAX_FILT];
+    orc_il il[ORC_MAX_IL];
+    int off[ORC_MAX_FILT + 1], nil[ORC_MAX_FILT], idx[ORC_MAX_FILT];
+    off[0] = 0;
     for (int i = 0; i < nf; ++i) {
-        nil[i] = filter_idx_l(P, f0 + i, p, l_in, il[i], ORC_MAX_IL);
-        if (nil[i] == 0) return;
+        const int n = filter_idx_l(P, f0 + i, p, l_in, il + off[i], ORC_MAX_IL - off[i]);
+        if (n < 0) { C->status = ORC_ERR_OVERFLOW; return; }
+        if (n == 0) return;
+        nil[i] = n;
+        off[i + 1] = off[i] + n;
         idx[i] = 0;
     }
     for (;;) {
         double l = ORC_MAX_F;
-        for (int i = 0; i < nf; ++i) l = l < il[i][idx[i]].l ? l : il[i][idx[i]].l;  /* std::min */
+        for (int i = 0; i < nf; ++i) {          /* l = std::min(l, x) */
+            const double x = il[off[i] + idx[i]].l;
+            l = (x < l) ? x : l;
+        }
         int idx1 = 0;
-        for (int i = 0; i < nf; ++i) idx1 += (int)(il[i][idx[i]].bin * fac[i + 1]);
+        for (int i = 0; i < nf; ++i) idx1 += (int)(il[off[i] + idx[i]].bin * fac[i + 1]);
         for (int s = 0; s < ns; ++s) {
             hist[idx1] += score_value(C, s0 + s, p, l);
             C->cnt[ORC_C_TALLY_UPDATES]++;
             idx1 += (int)fac[0];
         }
         for (int i = 0; i < nf; ++i) {
-            il[i][idx[i]].l -= l;
-            if (il[i][idx[i]].l < ORC_EPS_F) {
+            orc_il *cur = &il[off[i] + idx[i]];
+            cur->l -= l;
+            if (cur->l < ORC_EPS_F) {
                 if (idx[i] == nil[i] - 1) return;
                 idx[i]++;
             }

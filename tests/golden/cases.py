@@ -29,8 +29,7 @@ SEED = 0x4D43
 def _tables(d, specs, n_points=400):
     """specs: list of (zaid, A, s0, Ec, c0); log-uniform grid 1e-5..2e7 eV."""
     os.makedirs(os.path.join(d, "xs_library"), exist_ok=True)
-    E = np.exp(np.linspace(np.log(1e-5), np.log(2e7), n_points))
-    E[0], E[-1] = 1e-5, 2e7
+    E = W.log_uniform_grid(1e-5, 2e7, n_points)
     for zaid, A, s0, Ec, c0 in specs:
         W.write_xs_table(os.path.join(d, "xs_library", zaid + ".txt"), A, E,
                          s0 / (1.0 + E / Ec), c0 * np.sqrt(0.0253 / E))

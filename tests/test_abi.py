@@ -1,0 +1,92 @@
+"""The C ABI boundary: the library loads, exports what include/mcgpu.h
+declares, and turns input errors into status codes (no GPU needed)."""
+import ctypes
+import os
+import re
+import tempfile
+
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+HEADER = os.path.join(ROOT, "include", "mcgpu.h")
+
+
+@pytest.fixture(scope="module")
+def L():
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "mc-old_gb300"))
+    import build as B
+    B.build()
+    import mcgpu
+    return mcgpu.lib()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for need in ("mc_problem_load_xml", "mc_problem_free", "mc_run", "mc_tally_read",
+                 "mc_tally_count", "mc_counters_read", "mc_report", "mc_last_error"):
+        assert need in names
+
+
+def test_library_exports_every_declared_symbol(L):
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_status_strings(L):
+    L.mc_status_string.restype = ctypes.c_char_p
+    assert L.mc_status_string(0) == b"MC_OK"
+    assert L.mc_status_string(4) == b"MC_ERR_LOST"
+
+
+def _load(L, d):
+    h = ctypes.c_void_p()
+    st = L.mc_problem_load_xml(os.fsencode(d), os.fsencode(os.path.join(d, "xs_library")), ctypes.byref(h))
+    msg = L.mc_last_error(h).decode() if h else ""
+    if h:
+        L.mc_problem_free(h)
+    return st, msg
+
+
+BAD_INPUTS = {
+    "unknown surface type": '<surfaces><torus name="t"/></surfaces>',
+    "fission": None,
+    "unknown material": '<cells><cell name="c" material="nope"/></cells>',
+    "ksearch": '<simulation><description samples="10"/><ksearch active_cycles="1" passive_cycles="1"/></simulation>',
+    "particle comb": '<population_control><particle_comb bank_max="10" teeth="5"/></population_control>',
+    "unresolved distribution": '<distributions><independentXYZ name="d" datatype="point" x="a" y="b" z="c"/></distributions>',
+    "malformed xml": '<surfaces><plane_x name="p" x="1"></surfaces>',
+}
+
+
+@pytest.mark.parametrize("case", list(BAD_INPUTS))
+def test_input_errors_are_status_codes(L, case):
+    with tempfile.TemporaryDirectory() as d:
+        body = BAD_INPUTS[case]
+        if case == "fission":
+            os.makedirs(os.path.join(d, "xs_library"))
+            with open(os.path.join(d, "xs_library", "092235.txt"), "w") as f:
+                f.write("235\n0 0\n0 0\n0 0\n1e-5 10 5 100 2.4 0\n2e7 4 0.1 1 2.6 0\n")
+            body = '<nuclides><nuclide name="U" ZAID="092235"/></nuclides>'
+        with open(os.path.join(d, "input.xml"), "w") as f:
+            f.write("<?xml version='1.0'?>\n" + body + "\n")
+        st, msg = _load(L, d)
+        assert st == 1, (st, msg)   # MC_ERR_INPUT, never an exit
+        assert msg
+
+
+def test_valid_input_parses_before_device_init(L):
+    import cases
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case("slab_features", d)
+        st, msg = _load(L, d)
+        # parses; without a GPU the only possible failure is the device
+        assert st in (0, 2), (st, msg)
+        if st == 2:
+            assert "CUDA" in msg or "device" in msg
