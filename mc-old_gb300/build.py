@@ -37,6 +37,7 @@ SOURCES = [
     ("mc_engine.cpp", "host"),
     ("mc_api.cpp", "host"),
     ("mc_report.cpp", "host"),
+    ("mc_evtables.cpp", "host"),
     ("mc_history.cu", "fp64"),
     ("mc_event.cu", "fast"),
 ]

@@ -1,17 +1,1088 @@
-// mc_event.cu -- mixed-precision event-based engine (placeholder).
+// mc_event.cu -- mixed-precision, event-based transport engine.
+//
+// The reference walks one particle at a time through general.cpp:177-211.
+// Here every CTA of a persistent grid owns a tile of particles held as a
+// structure of arrays in shared memory and advances all of them one event
+// per iteration:
+//
+//   refill   free slots take a split copy from the CTA's overflow bank (SoA
+//            in HBM) or, when that is empty, a new history from the global
+//            history counter (one atomic per CTA per iteration);
+//   advance  every live particle: cross-section lookup, distance to
+//            collision, distance to the cell's surfaces, flight, track-length
+//            tallies; the particle joins the collision or the crossing queue
+//            (warp ballot + popc prefix, one shared atomic per warp);
+//   collide  the collision queue, dense: collision tallies, implicit capture,
+//            scatter nuclide, free-gas elastic scatter (or multigroup
+//            transfer), weight roulette;
+//   cross    the crossing queue, dense: new cell, boundary condition,
+//            crossing tallies, importance roulette / splitting, weight
+//            roulette.
+//
+// Tracking is FP32: positions, directions, energy, weight, distances and
+// cross-section interpolation.  Sphere and cylinder roots take the constant
+// term |p - c|^2 - r^2 as a compensated FP32 pair (error-free products and
+// sums) where cancellation bites, and use the stable quadratic form.  The
+// surface just crossed is known exactly ("coincident" surface) instead of the
+// reference's FLT_EPSILON nudge and all-cell search (general.cpp:94-96),
+// which FP32 positions cannot resolve: the new cell is searched among the
+// cells that list that surface with the opposite sense.  Tallies accumulate
+// in FP64: per history into L2-resident rows (one row per tile history slot,
+// with a touched-bin mask), folded into per-CTA shared sums when the
+// history's last particle dies, and into the global sums once per CTA.
+// Physics and tally semantics follow the reference line by line as the FP64
+// path does (see mc_history.cu); only the precision and the crossing logic
+// differ, so results agree statistically, not bit for bit.
+#include <cfloat>
+
 #include "mc_engine.h"
+#include "mc_evtables.h"
+#include "mc_math.cuh"
 
 namespace mc {
 
-struct EventState {};
+struct EventState {
+    EvHost host;
+    void *d_blob = nullptr;
+    EvTables dv{};
+    DevBuf acc, mask, ovf, misc;
+    int grid = 0, block = 0, tile = 0, ovf_cap = 0;
+    size_t smem = 0;
+    bool rows_dirty = true;
+};
 
-void event_state_free(EventState *s) { delete s; }
-
-mc_status run_event(const Tables &, DeviceProblem &, uint64_t, uint64_t, uint64_t, const mc_tune *,
-                    std::string &err)
+void event_state_free(EventState *s)
 {
-    err = "the mixed-precision event engine is not available in this build";
-    return MC_ERR_ARG;
+    if (!s) return;
+    if (s->d_blob) cudaFree(s->d_blob);
+    devbuf_free(s->acc);
+    devbuf_free(s->mask);
+    devbuf_free(s->ovf);
+    devbuf_free(s->misc);
+    delete s;
+}
+
+namespace {
+
+constexpr float kPiF = 3.14159265358979f;
+constexpr float k2PiF = 6.28318530717959f;
+constexpr float kPiHalfF = 1.57079632679490f;
+constexpr float kSqrtPiF = 1.77245385090552f;
+constexpr float kEpsF = FLT_EPSILON;
+constexpr float kInf = __builtin_huge_valf();
+constexpr int kMaxFilt = 8;
+constexpr int kMaxIl = 32;
+
+enum { C_FLIGHTS = 0, C_COLL, C_CROSS, C_TALLY, C_PART, C_SPLIT, C_XS, C_FREEGAS, C_NUC };
+
+// one particle between phases: split copies wait here (overflow bank, HBM)
+struct OvfP {
+    float x, y, z, u, v, w, E, wt, t;
+    int cell, surf, hslot, g;
+    uint32_t id;
+};
+
+struct EvArgs {
+    uint64_t first, n, seed;
+    unsigned long long *next;     // histories handed out (relative)
+    double *acc;                  // [grid * tile][nb]
+    unsigned long long *mask;     // [grid * tile][nw]
+    int nw;
+    OvfP *ovf;                    // [grid][ovf_cap]
+    int ovf_cap;
+    double *sum, *sq;             // global tallies
+    unsigned long long *counters;
+    int *status;
+    int tile;
+    int smem_sums;                // per-CTA sums live in shared memory
+};
+
+// Philox stream of one particle and event, FP32 draws (4 per block)
+struct Rng32 {
+    uint32_t k0, k1, hlo, id, ev, draw, cached;
+    U4 blk;
+    __device__ __forceinline__ void init(uint64_t seed, uint64_t hist, uint32_t pid, uint32_t event, uint32_t d)
+    {
+        k0 = (uint32_t)seed;
+        k1 = (uint32_t)(seed >> 32) ^ (uint32_t)(hist >> 32);
+        hlo = (uint32_t)hist;
+        id = pid;
+        ev = event;
+        draw = d;
+        cached = 0;
+    }
+    __device__ __forceinline__ float next()
+    {
+        const uint32_t b = draw >> 2;
+        if (cached != b + 1) {
+            blk = philox(b | 0x80000000u, ev, id, hlo, k0, k1);
+            cached = b + 1;
+        }
+        const uint32_t q = draw & 3u;
+        const uint32_t word = q == 0 ? blk.x : (q == 1 ? blk.y : (q == 2 ? blk.z : blk.w));
+        ++draw;
+        return u01f(word);
+    }
+};
+
+// shared-memory tile (SoA) and per-CTA bookkeeping
+struct Tile {
+    float *x, *y, *z, *u, *v, *w, *E, *wt, *t, *sig, *frac;
+    int *cell, *surf, *hs, *g, *gi, *sense;
+    uint32_t *id, *ev;
+    unsigned short *qc, *qx;
+    unsigned long long *hidx;
+    int *live, *hfree;
+    double *ssum, *ssq;
+};
+
+struct PState {
+    float x, y, z, u, v, w, E, wt, t;
+    int cell, surf, hslot, g;
+    uint32_t id, ev;
+};
+
+__device__ __forceinline__ void load_p(const Tile &T, int s, PState &p)
+{
+    p.x = T.x[s]; p.y = T.y[s]; p.z = T.z[s]; p.u = T.u[s]; p.v = T.v[s]; p.w = T.w[s];
+    p.E = T.E[s]; p.wt = T.wt[s]; p.t = T.t[s];
+    p.cell = T.cell[s]; p.surf = T.surf[s]; p.hslot = T.hs[s]; p.g = T.g[s];
+    p.id = T.id[s]; p.ev = T.ev[s];
+}
+
+__device__ __forceinline__ void store_p(const Tile &T, int s, const PState &p)
+{
+    T.x[s] = p.x; T.y[s] = p.y; T.z[s] = p.z; T.u[s] = p.u; T.v[s] = p.v; T.w[s] = p.w;
+    T.E[s] = p.E; T.wt[s] = p.wt; T.t[s] = p.t;
+    T.cell[s] = p.cell; T.surf[s] = p.surf; T.hs[s] = p.hslot; T.g[s] = p.g;
+    T.id[s] = p.id; T.ev[s] = p.ev;
+}
+
+struct Ctx {
+    const EvTables *V;
+    const EvArgs *A;
+    Tile T;
+    unsigned long long cnt[kNumCounters];
+    int *s_status;
+    int *s_novf;
+    int *s_nlive;
+    int *s_nhfree;
+    int nb;
+};
+
+// ---------------------------------------------------------------------------
+// cross sections
+// ---------------------------------------------------------------------------
+struct XsAt { int m, i; float f; };
+
+__device__ __forceinline__ XsAt xs_locate(const EvTables &V, int m, float E)
+{
+    const int off = V.mgrid_off[m], L = V.mgrid_len[m];
+    const float *g = V.gE + off;
+    if (E <= __ldg(g)) return XsAt{m, off, 0.f};
+    if (E >= __ldg(g + L - 1)) return XsAt{m, off + L - 2, 1.f};
+    int b = (int)((__log2f(E) - V.bkt_lo[m]) * V.bkt_inv[m]);
+    b = b < 0 ? 0 : (b >= V.bkt_n[m] ? V.bkt_n[m] - 1 : b);
+    int i = __ldg(V.bkt + V.bkt_off[m] + b);
+    while (i > 0 && __ldg(g + i) > E) --i;
+    while (__ldg(g + i + 1) < E) ++i;
+    const float e0 = __ldg(g + i), e1 = __ldg(g + i + 1);
+    return XsAt{m, off + i, (E - e0) / (e1 - e0)};
+}
+
+__device__ __forceinline__ float xs_at(const float *tab, const XsAt &a)
+{
+    const float y0 = __ldg(tab + a.i), y1 = __ldg(tab + a.i + 1);
+    return fmaf(a.f, y1 - y0, y0);
+}
+
+enum { XT = 0, XS = 1, XC = 2 };
+
+// macroscopic cross section of cell material at the particle's energy/group
+__device__ __forceinline__ float macro(Ctx &C, int m, int which, const PState &p)
+{
+    const EvTables &V = *C.V;
+    C.cnt[C_XS]++;
+    if (V.G > 0) {
+        const int i = m * V.G + p.g;
+        return which == XT ? __ldg(V.mg_total + i) : (which == XS ? __ldg(V.mg_scat_tot + i) : __ldg(V.mg_capture + i));
+    }
+    const XsAt a = xs_locate(V, m, p.E);
+    return xs_at(which == XT ? V.gT : (which == XS ? V.gS : V.gC), a);
+}
+
+// ---------------------------------------------------------------------------
+// geometry (FP32, coincident-surface aware)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float surface_eval(const EvTables &V, int s, float x, float y, float z)
+{
+    const float *k = V.surf_coef + 8 * s;
+    switch (V.surf_type[s]) {
+    case 0: return x - k[0];
+    case 1: return y - k[0];
+    case 2: return z - k[0];
+    case 3: return k[0] * x + k[1] * y + k[2] * z - k[3];
+    case 4: { const float a = x - k[0], b = y - k[1], c = z - k[2]; return a * a + b * b + c * c - k[4]; }
+    case 5: { const float a = y - k[0], b = z - k[1]; return a * a + b * b - k[3]; }
+    case 6: { const float a = x - k[0], b = y - k[1]; return a * a + b * b - k[3]; }  // cylinder_y as the reference evaluates it
+    default: { const float a = x - k[0], b = y - k[1]; return a * a + b * b - k[3]; }
+    }
+}
+
+// a*a + b*b (+ c*c) - r2 with error-free products and sums (Dekker / Knuth)
+__device__ __forceinline__ float comp_sumsq(float a, float b, float c, float r2)
+{
+    const float pa = a * a, ea = fmaf(a, a, -pa);
+    const float pb = b * b, eb = fmaf(b, b, -pb);
+    const float pc = c * c, ec = fmaf(c, c, -pc);
+    float s = pa + pb;
+    float bb = s - pa;
+    float err = (pa - (s - bb)) + (pb - bb);
+    float s2 = s + pc;
+    bb = s2 - s;
+    err += (s - (s2 - bb)) + (pc - bb);
+    float s3 = s2 - r2;
+    bb = s3 - s2;
+    err += (s2 - (s3 - bb)) + (-r2 - bb);
+    return s3 + (err + ea + eb + ec);
+}
+
+// smallest positive root of a t^2 + 2 h t + c = 0 (stable form)
+__device__ __forceinline__ float quad_root(float a, float h, float c, bool on)
+{
+    if (fabsf(a) < 1e-12f) return kInf;
+    if (on) {                       // c == 0: roots 0 and -2h/a
+        const float t = -2.f * h / a;
+        return t > 0.f ? t : kInf;
+    }
+    const float D = h * h - a * c;
+    if (D <= 0.f) return kInf;
+    const float sq = sqrtf(D);
+    const float q = -(h + copysignf(sq, h));
+    float t1 = q / a, t2 = (q != 0.f) ? c / q : kInf;
+    t1 = t1 > 0.f ? t1 : kInf;
+    t2 = t2 > 0.f ? t2 : kInf;
+    return fminf(t1, t2);
+}
+
+__device__ float surface_distance(const EvTables &V, int s, const PState &p, bool on)
+{
+    const float *k = V.surf_coef + 8 * s;
+    switch (V.surf_type[s]) {
+    case 0: case 1: case 2: {
+        if (on) return kInf;
+        const int ax = V.surf_type[s];
+        const float pos = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
+        const float dir = ax == 0 ? p.u : (ax == 1 ? p.v : p.w);
+        if (fabsf(dir) > kEpsF) {
+            const float d = (k[0] - pos) / dir;
+            return d > 0.f ? d : kInf;
+        }
+        return kInf;
+    }
+    case 3: {
+        if (on) return kInf;
+        const float den = k[0] * p.u + k[1] * p.v + k[2] * p.w;
+        if (fabsf(den) > kEpsF) {
+            const float d = (k[3] - k[0] * p.x - k[1] * p.y - k[2] * p.z) / den;
+            return d > 0.f ? d : kInf;
+        }
+        return kInf;
+    }
+    case 4: {
+        const float dx = p.x - k[0], dy = p.y - k[1], dz = p.z - k[2];
+        const float h = dx * p.u + dy * p.v + dz * p.w;
+        const float c = on ? 0.f : comp_sumsq(dx, dy, dz, k[4]);
+        return quad_root(1.f, h, c, on);
+    }
+    case 5: {
+        const float dy = p.y - k[0], dz = p.z - k[1];
+        const float h = dy * p.v + dz * p.w;
+        const float c = on ? 0.f : comp_sumsq(dy, dz, 0.f, k[3]);
+        return quad_root(1.f - p.u * p.u, h, c, on);
+    }
+    case 6: {
+        const float dx = p.x - k[0], dz = p.z - k[1];
+        const float h = dx * p.u + dz * p.w;
+        const float c = on ? 0.f : comp_sumsq(dx, dz, 0.f, k[3]);
+        return quad_root(1.f - p.v * p.v, h, c, on);
+    }
+    default: {
+        const float dx = p.x - k[0], dy = p.y - k[1];
+        const float h = dx * p.u + dy * p.v;
+        const float c = on ? 0.f : comp_sumsq(dx, dy, 0.f, k[3]);
+        return quad_root(1.f - p.w * p.w, h, c, on);
+    }
+    }
+}
+
+__device__ void surface_reflect(const EvTables &V, int s, PState &p)
+{
+    const float *k = V.surf_coef + 8 * s;
+    switch (V.surf_type[s]) {
+    case 0: p.u = -p.u; break;
+    case 1: p.v = -p.v; break;
+    case 2: p.w = -p.w; break;
+    case 3: {
+        const float K = k[0] * p.u + k[1] * p.v + k[2] * p.w;
+        p.u -= k[4] * K; p.v -= k[5] * K; p.w -= k[6] * K;
+        break;
+    }
+    default: break;   // the reference leaves quadric reflection a no-op (Geometry.cpp:219-222)
+    }
+}
+
+__device__ __forceinline__ bool cell_contains(const EvTables &V, int c, const PState &p, int S, bool pos_side)
+{
+    for (int i = V.cell_surf_off[c]; i < V.cell_surf_off[c + 1]; ++i) {
+        const int s2 = V.cell_surf[i];
+        const int sense = V.cell_sense[i];
+        if (s2 == S) {
+            if (sense != 0 && ((sense > 0) != pos_side)) return false;
+            continue;
+        }
+        if (surface_eval(V, s2, p.x, p.y, p.z) * (float)sense < 0.f) return false;
+    }
+    return true;
+}
+
+// cell on the far side of surface S (crossed to the positive side if pos)
+__device__ int cell_across(const EvTables &V, const PState &p, int S, bool pos)
+{
+    const int li = 2 * S + (pos ? 1 : 0);
+    for (int k = V.nb_off[li]; k < V.nb_off[li + 1]; ++k) {
+        const int c = V.nb_cell[k];
+        if (cell_contains(V, c, p, S, pos)) return c;
+    }
+    for (int c = 0; c < V.n_cell; ++c)
+        if (cell_contains(V, c, p, S, pos)) return c;
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+// tallies (FP32 scores, FP64 per-history accumulation)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int bsearch_f(float x, const float *vec, int n)
+{
+    int left = 0, right = n - 1;
+    while (left <= right) {
+        const int mid = (left + right) >> 1;
+        if (__ldg(vec + mid) < x) left = mid + 1;
+        else right = mid - 1;
+    }
+    return right;
+}
+
+struct Il { int bin; float l; };
+
+__device__ int filter_idx_l(const EvTables &V, int f, const PState &p, float t_old, float speed, float l,
+                            Il *out, int cap)
+{
+    const float *grid = V.filt_grid + V.filt_grid_off[f];
+    const int glen = V.filt_grid_len[f];
+    const int nbin = glen - 1;
+    switch (V.filt_kind[f]) {
+    case 0: {
+        const int b = bsearch_f((float)p.surf, grid, glen) + 1;
+        if (b < 0 || b >= V.filt_size[f]) return 0;
+        out[0].bin = b; out[0].l = l; return 1;
+    }
+    case 1: {
+        const int b = bsearch_f((float)p.cell, grid, glen) + 1;
+        if (b < 0 || b >= V.filt_size[f]) return 0;
+        out[0].bin = b; out[0].l = l; return 1;
+    }
+    case 2: {
+        const int b = bsearch_f(p.E, grid, glen);
+        if (b < 0 || b >= nbin) return 0;
+        out[0].bin = b; out[0].l = l; return 1;
+    }
+    case 4:
+        out[0].bin = p.g; out[0].l = l; return 1;
+    default: {
+        const int loc1 = bsearch_f(t_old, grid, glen), loc2 = bsearch_f(p.t, grid, glen);
+        if (loc1 == loc2) {
+            if (loc1 >= 0 && loc1 < nbin) { out[0].bin = loc1; out[0].l = l; return 1; }
+            return 0;
+        }
+        const int num_bin = loc2 - loc1 - 1;
+        const int need = (loc1 >= 0) + (num_bin > 0 ? num_bin : 0) + (loc2 < nbin);
+        if (need > cap) return -1;
+        int n = 0;
+        if (loc1 >= 0) { out[n].bin = loc1; out[n].l = (__ldg(grid + loc1 + 1) - t_old) * speed; ++n; }
+        for (int i = 1; i <= num_bin; ++i) {
+            out[n].bin = loc1 + i; out[n].l = (__ldg(grid + loc1 + i + 1) - __ldg(grid + loc1 + i)) * speed; ++n;
+        }
+        if (loc2 < nbin) { out[n].bin = loc2; out[n].l = (p.t - __ldg(grid + loc2)) * speed; ++n; }
+        return n;
+    }
+    }
+}
+
+__device__ __forceinline__ void tally_add(Ctx &C, int hslot, int bin, double val)
+{
+    const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
+    atomicAdd(C.A->acc + row * C.nb + bin, val);
+    unsigned long long *mw = C.A->mask + row * C.A->nw + (bin >> 6);
+    const unsigned long long bit = 1ull << (bin & 63);
+    if (!(*(volatile unsigned long long *)mw & bit)) atomicOr(mw, bit);
+    C.cnt[C_TALLY]++;
+}
+
+__device__ float score_value(Ctx &C, int sc, const PState &p, float l)
+{
+    const EvTables &V = *C.V;
+    const int m = V.cell_mat[p.cell];
+    float k;
+    switch (V.score_kernel[sc]) {
+    case 0: k = p.wt * l; break;
+    case 1: k = p.wt / (m >= 0 ? macro(C, m, XT, p) : 0.f); break;
+    default: k = p.wt; break;
+    }
+    switch (V.score_kind[sc]) {
+    case 0: return k;
+    case 1: case 3: return (m >= 0 ? macro(C, m, XC, p) : 0.f) * k;
+    case 2: return (m >= 0 ? macro(C, m, XS, p) : 0.f) * k;
+    default: return (m >= 0 ? macro(C, m, XT, p) : 0.f) * k;
+    }
+}
+
+// Estimator::score (Estimator.cpp:298-336)
+__device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, float speed, float l_in)
+{
+    const EvTables &V = *C.V;
+    const int f0 = V.est_filt_off[e], nf = V.est_filt_off[e + 1] - f0;
+    const int s0 = V.est_score_off[e], ns = V.est_score_off[e + 1] - s0;
+    const int *fac = V.est_factor + V.est_factor_off[e];
+    const int base = V.est_bin_off[e];
+    Il il[kMaxIl];
+    int off[kMaxFilt + 1], nil[kMaxFilt], idx[kMaxFilt];
+    off[0] = 0;
+    for (int i = 0; i < nf; ++i) {
+        const int n = filter_idx_l(V, f0 + i, p, t_old, speed, l_in, il + off[i], kMaxIl - off[i]);
+        if (n < 0) { atomicCAS(C.s_status, 0, DS_OVERFLOW); return; }
+        if (n == 0) return;
+        nil[i] = n;
+        off[i + 1] = off[i] + n;
+        idx[i] = 0;
+    }
+    for (;;) {
+        float l = FLT_MAX;
+        for (int i = 0; i < nf; ++i) { const float x = il[off[i] + idx[i]].l; l = (x < l) ? x : l; }
+        int idx1 = 0;
+        for (int i = 0; i < nf; ++i) idx1 += il[off[i] + idx[i]].bin * fac[i + 1];
+        for (int s = 0; s < ns; ++s) {
+            tally_add(C, p.hslot, base + idx1, (double)score_value(C, s0 + s, p, l));
+            idx1 += fac[0];
+        }
+        for (int i = 0; i < nf; ++i) {
+            Il &cur = il[off[i] + idx[i]];
+            cur.l -= l;
+            if (cur.l < kEpsF) {
+                if (idx[i] == nil[i] - 1) return;
+                idx[i]++;
+            }
+        }
+        if (nf == 0) return;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// particle life cycle
+// ---------------------------------------------------------------------------
+__device__ void history_fold(Ctx &C, int hslot)
+{
+    const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
+    double *acc = C.A->acc + row * C.nb;
+    unsigned long long *mask = C.A->mask + row * C.A->nw;
+    for (int wi = 0; wi < C.A->nw; ++wi) {
+        if (__ldcg(mask + wi) == 0ull) continue;
+        unsigned long long m = atomicExch(mask + wi, 0ull);
+        while (m) {
+            const int b = __ffsll((long long)m) - 1;
+            m &= m - 1;
+            const int bin = wi * 64 + b;
+            const double v = __longlong_as_double(
+                (long long)atomicExch(reinterpret_cast<unsigned long long *>(acc + bin), 0ull));
+            if (C.A->smem_sums) {
+                atomicAdd(C.T.ssum + bin, v);
+                atomicAdd(C.T.ssq + bin, v * v);
+            } else {
+                atomicAdd(C.A->sum + bin, v);
+                atomicAdd(C.A->sq + bin, v * v);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void particle_dies(Ctx &C, int s, int hslot)
+{
+    C.T.hs[s] = -1;
+    atomicSub(C.s_nlive, 1);
+    if (atomicSub(&C.T.live[hslot], 1) == 1) {
+        __threadfence_block();
+        history_fold(C, hslot);
+        const int k = atomicAdd(C.s_nhfree, 1);
+        C.T.hfree[k] = hslot;
+    }
+}
+
+__device__ __forceinline__ float speed_of(float E) { return 1383159.26439f * sqrtf(E); }
+
+// Algorithm.cpp:67-101 in FP32
+__device__ __forceinline__ void scatter_direction(Rng32 &R, float dx, float dy, float dz, float mu0,
+                                                  float &ox, float &oy, float &oz)
+{
+    float sa, ca;
+    __sincosf(k2PiF * R.next(), &sa, &ca);
+    const float Ac = sqrtf(fmaxf(1.f - mu0 * mu0, 0.f));
+    if (dz != 1.f) {
+        const float B = sqrtf(fmaxf(1.f - dz * dz, 0.f));
+        const float Cc = Ac / B;
+        ox = dx * mu0 + (dx * dz * ca - dy * sa) * Cc;
+        oy = dy * mu0 + (dy * dz * ca + dx * sa) * Cc;
+        oz = dz * mu0 - ca * Ac * B;
+    } else {
+        const float B = sqrtf(fmaxf(1.f - dy * dy, 0.f));
+        const float Cc = Ac / B;
+        ox = dx * mu0 + (dx * dy * ca - dz * sa) * Cc;
+        oz = dz * mu0 + (dz * dy * ca + dx * sa) * Cc;
+        oy = dy * mu0 - ca * Ac * B;
+    }
+}
+
+// Reaction.cpp:27-118 in FP32
+__device__ bool free_gas(Ctx &C, Rng32 &R, PState &p, float A)
+{
+    const float mu0 = 2.f * R.next() - 1.f;
+    const float speed = speed_of(p.E);
+    const float beta = sqrtf(2.0659834e-11f * A);
+    const float y = beta * speed;
+    const float p_g2 = 2.f / (2.f + kSqrtPiF * y);
+    float V, mu;
+    for (int it = 0;; ++it) {
+        C.cnt[C_FREEGAS]++;
+        if (it > (1 << 16)) return false;
+        float x;
+        if (R.next() < p_g2) {
+            const float a = R.next(), b = R.next();
+            x = sqrtf(-__logf(a * b));
+        } else {
+            const float cv = __cosf(kPiHalfF * R.next());
+            const float u1 = R.next(), u2 = R.next();
+            x = sqrtf(-__logf(u1) - __logf(u2) * cv * cv);
+        }
+        V = x / beta;
+        mu = 2.f * R.next() - 1.f;
+        const float acc = sqrtf(fmaxf(speed * speed + V * V - 2.f * speed * V * mu, 0.f)) / (speed + V);
+        if (!(R.next() > acc)) break;
+    }
+    float nx, ny, nz;
+    scatter_direction(R, p.u, p.v, p.w, mu, nx, ny, nz);
+    const float inv = 1.f / (1.f + A);
+    const float ux = (speed * p.u + A * (nx * V)) * inv;
+    const float uy = (speed * p.v + A * (ny * V)) * inv;
+    const float uz = (speed * p.w + A * (nz * V)) * inv;
+    const float cx = speed * p.u - ux, cy = speed * p.v - uy, cz = speed * p.w - uz;
+    const float sc = sqrtf(cx * cx + cy * cy + cz * cz);
+    const float isc = 1.f / sc;
+    float dx, dy, dz;
+    scatter_direction(R, cx * isc, cy * isc, cz * isc, mu0, dx, dy, dz);
+    const float vx = sc * dx + ux, vy = sc * dy + uy, vz = sc * dz + uz;
+    const float vs = sqrtf(vx * vx + vy * vy + vz * vz);
+    const float ivs = 1.f / vs;
+    p.E = 5.2270376e-13f * vs * vs;
+    p.u = vx * ivs; p.v = vy * ivs; p.w = vz * ivs;
+    return true;
+}
+
+__device__ __forceinline__ void weight_roulette(Ctx &C, Rng32 &R, PState &p, bool &alive)
+{
+    if (p.wt < C.V->wr) {
+        if (R.next() < p.wt / C.V->ws) p.wt = C.V->ws;
+        else alive = false;
+    }
+}
+
+// SourceBank / SourcePoint (Source.cpp:20-24, 42-45), FP32
+__device__ void sample_source(const EvTables &V, uint64_t seed, uint64_t hist, PState &p)
+{
+    Rng32 R;
+    R.init(seed, hist, 0u, 0u, 0u);
+    const float xi = R.next();
+    int s = bsearch_f(xi, V.src_cdf, V.n_src + 1);
+    s = s < 0 ? 0 : (s >= V.n_src ? V.n_src - 1 : s);
+    const float *ep = V.src_e_par + 2 * s;
+    const float E = (V.src_e_kind[s] == 1) ? ep[0] + R.next() * ep[1] : ep[0];
+    const float *dp = V.src_dir_par + 9 * s;
+    const int dk = V.src_dir_kind[s];
+    float d0, d1, d2;
+    if (dk == 0) {
+        d0 = dp[0]; d1 = dp[1]; d2 = dp[2];
+    } else if (dk == 1 || dk == 3) {
+        const float mu = (dk == 1) ? 2.f * R.next() - 1.f : R.next();
+        float sa, ca;
+        __sincosf(k2PiF * R.next(), &sa, &ca);
+        const float c = sqrtf(fmaxf(1.f - mu * mu, 0.f));
+        d0 = mu; d1 = ca * c; d2 = sa * c;
+    } else {
+        float d[3];
+        for (int k = 2; k >= 0; --k) {
+            const float *q = dp + 3 * k;
+            d[k] = ((int)q[0] == 1) ? q[1] + R.next() * q[2] : q[1];
+        }
+        d0 = d[0]; d1 = d[1]; d2 = d[2];
+    }
+    p.x = V.src_pos[3 * s]; p.y = V.src_pos[3 * s + 1]; p.z = V.src_pos[3 * s + 2];
+    p.u = d0; p.v = d1; p.w = d2;
+    p.E = E; p.wt = 1.f; p.t = 0.f;
+    p.cell = V.src_cell[s];
+    p.surf = -1;
+    p.g = V.src_group[s];
+    p.id = 0u;
+    p.ev = 0u;
+}
+
+// ---------------------------------------------------------------------------
+// the persistent kernel
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int warp_append(int *counter, bool pred)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        if (lane == leader) base = atomicAdd(counter, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int P = A.tile;
+    const int H = P;
+    // carve the tile
+    Tile T;
+    {
+        unsigned char *q = smem;
+        auto takef = [&](float *&ptr) { ptr = reinterpret_cast<float *>(q); q += sizeof(float) * P; };
+        auto takei = [&](int *&ptr) { ptr = reinterpret_cast<int *>(q); q += sizeof(int) * P; };
+        double *d = reinterpret_cast<double *>(q);
+        T.ssum = d; T.ssq = d + (A.smem_sums ? V.n_bins : 0);
+        q += sizeof(double) * (A.smem_sums ? 2 * V.n_bins : 0);
+        T.hidx = reinterpret_cast<unsigned long long *>(q); q += sizeof(unsigned long long) * H;
+        takef(T.x); takef(T.y); takef(T.z); takef(T.u); takef(T.v); takef(T.w);
+        takef(T.E); takef(T.wt); takef(T.t); takef(T.sig); takef(T.frac);
+        takei(T.cell); takei(T.surf); takei(T.hs); takei(T.g); takei(T.gi); takei(T.sense);
+        T.id = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
+        T.ev = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
+        takei(T.live); takei(T.hfree);
+        T.qc = reinterpret_cast<unsigned short *>(q); q += sizeof(unsigned short) * P;
+        T.qx = reinterpret_cast<unsigned short *>(q); q += sizeof(unsigned short) * P;
+    }
+    __shared__ int s_nlive, s_novf, s_nhfree, s_status, s_nqc, s_nqx, s_rank;
+    __shared__ int s_take_ovf, s_got, s_ovf_base, s_hfree_base, s_exhausted;
+    __shared__ unsigned long long s_hist_base;
+
+    Ctx C;
+    C.V = &V;
+    C.A = &A;
+    C.T = T;
+    C.s_status = &s_status;
+    C.s_novf = &s_novf;
+    C.s_nlive = &s_nlive;
+    C.s_nhfree = &s_nhfree;
+    C.nb = (int)V.n_bins;
+    for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
+
+    for (int s = threadIdx.x; s < P; s += blockDim.x) {
+        T.hs[s] = -1;
+        T.hfree[s] = s;
+        T.live[s] = 0;
+    }
+    if (A.smem_sums)
+        for (int b = threadIdx.x; b < 2 * V.n_bins; b += blockDim.x) T.ssum[b] = 0.0;
+    if (threadIdx.x == 0) {
+        s_nlive = 0; s_novf = 0; s_nhfree = H; s_status = 0; s_nqc = 0; s_nqx = 0;
+        s_exhausted = 0;
+    }
+    __syncthreads();
+    OvfP *ovf = A.ovf + (size_t)blockIdx.x * A.ovf_cap;
+
+    for (;;) {
+        // ---------------- refill ----------------
+        if (threadIdx.x == 0) {
+            const int free_slots = P - s_nlive;
+            const int take = min(free_slots, s_novf);
+            s_take_ovf = take;
+            s_ovf_base = s_novf - take;
+            s_novf -= take;
+            int need = free_slots - take;
+            int got = 0;
+            if (need > 0 && s_novf == 0 && !s_exhausted && s_status == 0) {
+                const unsigned long long g0 = atomicAdd(A.next, (unsigned long long)need);
+                if (g0 >= A.n) {
+                    s_exhausted = 1;
+                } else {
+                    got = (int)min((unsigned long long)need, A.n - g0);
+                    if (g0 + (unsigned long long)need >= A.n) s_exhausted = 1;
+                }
+                s_hist_base = g0;
+            }
+            s_got = got;
+            s_nhfree -= got;
+            s_hfree_base = s_nhfree;
+            s_nlive += take + got;
+            s_rank = 0;
+        }
+        __syncthreads();
+        if (s_nlive == 0 && s_novf == 0 && (s_exhausted || s_status != 0)) break;
+        if (s_status != 0) break;
+        for (int s0 = 0; s0 < P; s0 += blockDim.x) {
+            const int s = s0 + threadIdx.x;
+            const bool is_free = s < P && T.hs[s] < 0;
+            const int r = warp_append(&s_rank, is_free);
+            if (!is_free) continue;
+            PState p;
+            if (r < s_take_ovf) {
+                const OvfP &o = ovf[s_ovf_base + r];
+                p.x = o.x; p.y = o.y; p.z = o.z; p.u = o.u; p.v = o.v; p.w = o.w;
+                p.E = o.E; p.wt = o.wt; p.t = o.t; p.cell = o.cell; p.surf = o.surf;
+                p.hslot = o.hslot; p.g = o.g; p.id = o.id; p.ev = 0u;
+                store_p(T, s, p);
+                C.cnt[C_PART]++;
+            } else if (r - s_take_ovf < s_got) {
+                const int k = r - s_take_ovf;
+                const int hslot = T.hfree[s_hfree_base + k];
+                const uint64_t hist = A.first + s_hist_base + (uint64_t)k;
+                T.hidx[hslot] = hist;
+                T.live[hslot] = 1;
+                sample_source(V, A.seed, hist, p);
+                p.hslot = hslot;
+                store_p(T, s, p);
+                C.cnt[C_PART]++;
+            }
+        }
+        __syncthreads();
+
+        // ---------------- advance ----------------
+        for (int s0 = 0; s0 < P; s0 += blockDim.x) {
+            const int s = s0 + threadIdx.x;
+            const bool live = s < P && T.hs[s] >= 0;
+            int kind = 0;   // 1 collide, 2 cross
+            if (live) {
+                PState p;
+                load_p(T, s, p);
+                p.ev += 1u;
+                Rng32 R;
+                R.init(A.seed, T.hidx[p.hslot], p.id, p.ev, 0u);
+                const int m = V.cell_mat[p.cell];
+                float sig = 0.f, dcol;
+                if (m >= 0) {
+                    sig = macro(C, m, XT, p);
+                    dcol = -__logf(R.next()) / sig;
+                } else {
+                    dcol = 0.9f * FLT_MAX;
+                }
+                float dist = kInf;
+                int S = -1, sense = 0;
+                for (int i = V.cell_surf_off[p.cell]; i < V.cell_surf_off[p.cell + 1]; ++i) {
+                    const int sf = V.cell_surf[i];
+                    const float d = surface_distance(V, sf, p, sf == p.surf);
+                    if (d < dist) { dist = d; S = sf; sense = V.cell_sense[i]; }
+                }
+                const bool cross = dcol > dist;
+                const float l = cross ? dist : dcol;
+                if (!cross || S >= 0) {
+                    const float speed = speed_of(p.E);
+                    const float t_old = p.t;
+                    p.x = fmaf(p.u, l, p.x); p.y = fmaf(p.v, l, p.y); p.z = fmaf(p.w, l, p.z);
+                    if (V.has_time) p.t = t_old + l / speed;
+                    C.cnt[C_FLIGHTS]++;
+                    if (m >= 0 && V.G == 0) C.cnt[C_NUC] += (unsigned long long)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
+                    for (int i = V.cell_tl_off[p.cell]; i < V.cell_tl_off[p.cell + 1]; ++i)
+                        estimator_score(C, V.cell_tl[i], p, t_old, speed, l);
+                    p.surf = -1;
+                    kind = cross ? 2 : 1;
+                    T.gi[s] = S;
+                    T.sense[s] = sense;
+                    T.sig[s] = sig;
+                } else {
+                    atomicCAS(&s_status, 0, DS_LOST);
+                }
+                store_p(T, s, p);
+            }
+            const int pc = warp_append(&s_nqc, kind == 1);
+            if (kind == 1) T.qc[pc] = (unsigned short)s;
+            const int px = warp_append(&s_nqx, kind == 2);
+            if (kind == 2) T.qx[px] = (unsigned short)s;
+        }
+        __syncthreads();
+
+        // ---------------- collide ----------------
+        const int nqc = s_nqc;
+        for (int j = threadIdx.x; j < nqc; j += blockDim.x) {
+            const int s = T.qc[j];
+            PState p;
+            load_p(T, s, p);
+            Rng32 R;
+            R.init(A.seed, T.hidx[p.hslot], p.id, p.ev, 1u);
+            C.cnt[C_COLL]++;
+            bool alive = true;
+            const int m = V.cell_mat[p.cell];
+            if (m < 0) {
+                alive = false;
+            } else {
+                for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
+                    estimator_score(C, V.cell_c[i], p, p.t, speed_of(p.E), 0.f);
+                const float st = T.sig[s];
+                if (V.G > 0) {
+                    const int row = m * V.G + p.g;
+                    p.wt = p.wt * (st - __ldg(V.mg_capture + row)) / st;
+                    const float *cdf = V.mg_cdf + (size_t)row * V.G;
+                    const float u = __ldg(cdf + V.G - 1) * R.next();
+                    int gout = -1;
+                    for (int g2 = 0; g2 < V.G; ++g2)
+                        if (__ldg(cdf + g2) > u) { gout = g2; break; }
+                    if (gout >= 0) {
+                        p.g = gout;
+                        const float mu = 2.f * R.next() - 1.f;
+                        float nx, ny, nz;
+                        scatter_direction(R, p.u, p.v, p.w, mu, nx, ny, nz);
+                        p.u = nx; p.v = ny; p.w = nz;
+                    }
+                    C.cnt[C_XS]++;
+                } else {
+                    const XsAt a = xs_locate(V, m, p.E);
+                    const float sc = xs_at(V.gC, a);
+                    const float ss = xs_at(V.gS, a);
+                    C.cnt[C_XS] += 2;
+                    p.wt = p.wt * (st - sc) / st;
+                    const float u = ss * R.next();
+                    float acc = 0.f;
+                    int nuc = -1;
+                    for (int k = V.mnuc_off[m]; k < V.mnuc_off[m + 1]; ++k) {
+                        acc += xs_at(V.nucS + V.mnuc_tab[k] - V.mgrid_off[m], a);
+                        if (acc > u) { nuc = V.mnuc_id[k]; break; }
+                    }
+                    if (nuc >= 0 && !free_gas(C, R, p, __ldg(V.nuc_A + nuc))) atomicCAS(&s_status, 0, DS_TIMEOUT);
+                }
+            }
+            if (alive) weight_roulette(C, R, p, alive);
+            if (alive) {
+                store_p(T, s, p);
+            } else {
+                particle_dies(C, s, p.hslot);
+            }
+        }
+
+        // ---------------- cross ----------------
+        const int nqx = s_nqx;
+        for (int j = threadIdx.x; j < nqx; j += blockDim.x) {
+            const int s = T.qx[j];
+            PState p;
+            load_p(T, s, p);
+            Rng32 R;
+            R.init(A.seed, T.hidx[p.hslot], p.id, p.ev, 1u);
+            C.cnt[C_CROSS]++;
+            const int S = T.gi[s];
+            const int old_cell = p.cell;
+            bool alive = true;
+            const int bc = V.surf_bc[S];
+            p.surf = S;
+            if (bc == 0) {
+                const bool pos = !(T.sense[s] > 0);
+                const int c = cell_across(V, p, S, pos);
+                if (c < 0) { atomicCAS(&s_status, 0, DS_LOST); alive = false; }
+                else p.cell = c;
+            } else if (bc == -1) {
+                alive = false;
+                p.wt = 0.f;
+            } else {
+                surface_reflect(V, S, p);
+            }
+            if (p.wt != 0.f) {   // a vacuum boundary kills first and scores zero (general.cpp:98-111)
+                const float speed = speed_of(p.E);
+                for (int i = V.surf_est_off[S]; i < V.surf_est_off[S + 1]; ++i)
+                    estimator_score(C, V.surf_est[i], p, p.t, speed, 0.f);
+            }
+            if (alive && p.cell != old_cell) {
+                // population_control.cpp:21-49
+                const float Iold = V.cell_imp[old_cell], Inew = V.cell_imp[p.cell];
+                if (Inew != Iold) {
+                    const float rat = Inew / Iold;
+                    if (rat < 1.f) {
+                        if (R.next() < rat) p.wt = p.wt / rat;
+                        else alive = false;
+                    } else {
+                        const int n = (int)floorf(rat + R.next());
+                        p.wt = p.wt / (float)n;
+                        for (int k = 1; k < n; ++k) {
+                            const int slot = atomicAdd(&s_novf, 1);
+                            if (slot >= A.ovf_cap) { atomicCAS(&s_status, 0, DS_OVERFLOW); break; }
+                            OvfP o;
+                            o.x = p.x; o.y = p.y; o.z = p.z; o.u = p.u; o.v = p.v; o.w = p.w;
+                            o.E = p.E; o.wt = p.wt; o.t = p.t; o.cell = p.cell; o.surf = p.surf;
+                            o.hslot = p.hslot; o.g = p.g;
+                            o.id = child_id(p.id, p.ev, (uint32_t)k);
+                            ovf[slot] = o;
+                            atomicAdd(&T.live[p.hslot], 1);
+                            C.cnt[C_SPLIT]++;
+                        }
+                    }
+                }
+            }
+            if (alive) weight_roulette(C, R, p, alive);
+            if (alive) store_p(T, s, p);
+            else particle_dies(C, s, p.hslot);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_nqc = 0;
+            s_nqx = 0;
+            if (s_novf > A.ovf_cap) s_novf = A.ovf_cap;
+        }
+        __syncthreads();
+    }
+
+    // flush per-CTA sums and counters
+    __syncthreads();
+    if (A.smem_sums) {
+        for (int b = threadIdx.x; b < V.n_bins; b += blockDim.x) {
+            const double sv = T.ssum[b], qv = T.ssq[b];
+            if (sv != 0.0) atomicAdd(A.sum + b, sv);
+            if (qv != 0.0) atomicAdd(A.sq + b, qv);
+        }
+    }
+    if (threadIdx.x == 0 && s_status != 0) atomicCAS(A.status, 0, s_status);
+    for (int i = 0; i < kNumCounters; ++i) {
+        unsigned long long v = C.cnt[i];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(A.counters + i, v);
+    }
+}
+
+size_t tile_smem_bytes(int P, long long nb, bool smem_sums)
+{
+    size_t b = 0;
+    b += smem_sums ? sizeof(double) * 2 * (size_t)nb : 0;
+    b += sizeof(unsigned long long) * P;
+    b += 11 * sizeof(float) * P;
+    b += 6 * sizeof(int) * P;
+    b += 2 * sizeof(uint32_t) * P;
+    b += 2 * sizeof(int) * P;
+    b += 2 * sizeof(unsigned short) * P;
+    return b + 64;
+}
+
+}  // namespace
+
+mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n, uint64_t seed,
+                    const mc_tune *tune, std::string &err)
+{
+    cudaError_t e;
+    if (!d.ev_state) {
+        EventState *S = new EventState();
+        if (!build_event_tables(t, S->host, err)) { delete S; return MC_ERR_INPUT; }
+        if ((e = cudaMalloc(&S->d_blob, S->host.blob.size())) != cudaSuccess) {
+            delete S;
+            err = cuda_msg(e, "cudaMalloc(event tables)");
+            return MC_ERR_NOMEM;
+        }
+        cudaMemcpy(S->d_blob, S->host.blob.data(), S->host.blob.size(), cudaMemcpyHostToDevice);
+        S->dv = S->host.view;
+        for (auto &f : S->host.fix) *f.first = static_cast<const char *>(S->d_blob) + f.second;
+        S->dv = S->host.view;
+        d.ev_state = S;
+    }
+    EventState &S = *d.ev_state;
+    const EvTables &V = S.dv;
+    const int block = (tune && tune->block) ? (int)tune->block : 256;
+    if (block != 256) { err = "the event kernel is built for 256-thread blocks"; return MC_ERR_ARG; }
+    int tile = (tune && tune->bank_capacity) ? (int)tune->bank_capacity : 512;
+    if (tile < block || tile % block != 0 || tile > 4096) { err = "tile (bank_capacity) must be a multiple of 256 up to 4096"; return MC_ERR_ARG; }
+    const long long nb = std::max<long long>(V.n_bins, 1);
+    const bool smem_sums = nb <= 4096;
+    const size_t smem = tile_smem_bytes(tile, nb, smem_sums);
+    if ((e = cudaFuncSetAttribute(k_event, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) {
+        err = cuda_msg(e, "event kernel shared memory");
+        return MC_ERR_ARG;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_event, block, smem);
+    if (per_sm < 1) { err = "event kernel does not fit on an SM with this tile"; return MC_ERR_ARG; }
+    int grid = (tune && tune->grid_blocks) ? (int)tune->grid_blocks : d.sms * per_sm;
+    const int nw = (int)((nb + 63) / 64);
+    const int ovf_cap = 4 * tile;
+    const size_t rows = (size_t)grid * tile;
+    const bool grow = !S.acc.ptr || S.acc.bytes < rows * nb * sizeof(double);
+    if (!devbuf_reserve(S.acc, rows * nb * sizeof(double)) ||
+        !devbuf_reserve(S.mask, rows * nw * sizeof(unsigned long long)) ||
+        !devbuf_reserve(S.ovf, (size_t)grid * ovf_cap * sizeof(OvfP)) ||
+        !devbuf_reserve(S.misc, 256 + kNumCounters * sizeof(unsigned long long))) {
+        err = "cannot allocate event-engine scratch";
+        return MC_ERR_NOMEM;
+    }
+    if (grow || S.rows_dirty) {
+        cudaMemsetAsync(S.acc.ptr, 0, rows * nb * sizeof(double), d.stream);
+        cudaMemsetAsync(S.mask.ptr, 0, rows * nw * sizeof(unsigned long long), d.stream);
+        S.rows_dirty = false;
+    }
+    char *misc = static_cast<char *>(S.misc.ptr);
+    cudaMemsetAsync(misc, 0, 256 + kNumCounters * sizeof(unsigned long long), d.stream);
+    EvArgs A;
+    A.first = first;
+    A.n = n;
+    A.seed = seed;
+    A.next = reinterpret_cast<unsigned long long *>(misc);
+    A.status = reinterpret_cast<int *>(misc + 8);
+    A.counters = reinterpret_cast<unsigned long long *>(misc + 64);
+    A.acc = static_cast<double *>(S.acc.ptr);
+    A.mask = static_cast<unsigned long long *>(S.mask.ptr);
+    A.nw = nw;
+    A.ovf = static_cast<OvfP *>(S.ovf.ptr);
+    A.ovf_cap = ovf_cap;
+    A.sum = d.d_sum;
+    A.sq = d.d_sq;
+    A.tile = tile;
+    A.smem_sums = smem_sums ? 1 : 0;
+    cudaEventRecord(d.ev[0], d.stream);
+    k_event<<<grid, block, smem, d.stream>>>(V, A);
+    if ((e = cudaGetLastError()) != cudaSuccess) { err = cuda_msg(e, "event kernel launch"); return MC_ERR_CUDA; }
+    cudaEventRecord(d.ev[1], d.stream);
+    int hs = 0;
+    unsigned long long cnt[kNumCounters];
+    if ((e = cudaMemcpyAsync(&hs, A.status, sizeof(int), cudaMemcpyDeviceToHost, d.stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(cnt, A.counters, sizeof(cnt), cudaMemcpyDeviceToHost, d.stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(d.stream)) != cudaSuccess) {
+        err = cuda_msg(e, "event kernel");
+        S.rows_dirty = true;
+        return MC_ERR_CUDA;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, d.ev[0], d.ev[1]);
+    if (hs != DS_OK) {
+        S.rows_dirty = true;
+        err = hs == DS_LOST ? "a particle was lost (no cell contains it)"
+            : hs == DS_OVERFLOW ? "split-particle bank or time-filter buffer overflow"
+            : hs == DS_TIMEOUT ? "free-gas rejection loop did not converge" : "device error status";
+        return status_from_device(hs);
+    }
+    mc_counters &L = d.last;
+    L.flights = cnt[0]; L.collisions = cnt[1]; L.crossings = cnt[2]; L.tally_updates = cnt[3];
+    L.particles = cnt[4]; L.splits = cnt[5]; L.xs_evals = cnt[6]; L.freegas_iters = cnt[7];
+    L.nuc_lookups = cnt[8];
+    L.histories = n;
+    L.transport_ms = ms;
+    L.fold_ms = 0.0;
+    L.total_ms = ms;
+    L.launches = 1;
+    d.histories += n;
+    d.ntrack += L.flights;
+    return MC_OK;
 }
 
 }  // namespace mc

@@ -1,0 +1,107 @@
+"""Mixed-precision event engine against FP64 replay and the CPU oracle.
+
+Production mode tracks in FP32 and crosses surfaces without the reference's
+FLT_EPSILON nudge, so it is compared statistically: every tally bin within
+combined 3 sigma of the FP64 result (allowing the 2 % of bins a fair test
+misses) and the chi-square over bins consistent with zero difference.  The
+FP64 replay it is compared with is itself bit-identical to the CPU oracle."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import cases
+from stats import assert_agree
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mc():
+    import build as B
+    B.build()
+    import mcgpu
+    return mcgpu
+
+
+def _run(mc, d, n, mode, xs=True, **kw):
+    p = mc.Problem(d, d + "/xs_library" if xs else None)
+    c = p.run(n=n, mode=mode, **kw)
+    m, s, _, _ = p.all_tallies()
+    p.close()
+    return m, s, c
+
+
+CASES = {
+    "ce_sphere_small": (lambda d: cases.write_case("ce_sphere_small", d), 20000),
+    "slab_features": (lambda d: cases.write_case("slab_features", d), 20000),
+    "quadrics": (lambda d: cases.write_case("quadrics", d), 20000),
+    "absorber_slab": (lambda d: cases.write_case("absorber_slab", d), 200000),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_event_agrees_with_fp64(mc, name):
+    writer, n = CASES[name]
+    with tempfile.TemporaryDirectory() as d:
+        writer(d)
+        m1, s1, c1 = _run(mc, d, n, "event")
+        m2, s2, c2 = _run(mc, d, n, "replay")
+    assert c1["histories"] == n
+    assert_agree(m1, s1, m2, s2, name)
+    # event counts agree to a few percent (same physics, different streams)
+    assert abs(c1["flights"] / c2["flights"] - 1) < 0.05
+
+
+def test_event_agrees_with_cpu_oracle(mc):
+    from oracle import problem as OP
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case("ce_sphere_small", d)
+        m1, s1, _ = _run(mc, d, 3000, "event")
+        r = OP.run(OP.load(d, xs_dir=d + "/xs_library"), n=3000)
+        m2, s2 = r.finalize()
+    assert_agree(m1, s1, m2, s2, "event vs CPU oracle")
+
+
+def _ext():
+    import mcgpu.workloads as W
+    return {
+        "slab_1g": (lambda d: W.slab_1g(d, samples=100, n_flux_bins=20), 100000),
+        "mg_deep_slab": (lambda d: W.mg_deep_slab(d, samples=100, G=8), 100000),
+        "mg_layered_slab": (lambda d: W.mg_layered_slab(d, samples=100), 100000),
+    }
+
+
+@pytest.mark.parametrize("name", ["slab_1g", "mg_deep_slab", "mg_layered_slab"])
+def test_event_agrees_with_fp64_extensions(mc, name):
+    writer, n = _ext()[name]
+    with tempfile.TemporaryDirectory() as d:
+        writer(d)
+        m1, s1, c1 = _run(mc, d, n, "event")
+        m2, s2, c2 = _run(mc, d, n, "replay")
+    assert_agree(m1, s1, m2, s2, name)
+
+
+def test_event_tiles_and_grids(mc):
+    """Other tile sizes and grid shapes give statistically equal answers and
+    every history is run exactly once."""
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case("slab_features", d)
+        ref = _run(mc, d, 20000, "event")
+        for tile, grid in ((256, 7), (1024, 0), (512, 1)):
+            m, s, c = _run(mc, d, 20000, "event", bank_capacity=tile, grid_blocks=grid)
+            assert c["histories"] == 20000
+            assert_agree(m, s, ref[0], ref[1], f"tile {tile} grid {grid}")
+
+
+def test_event_overflow_is_a_status(mc):
+    """A tiny overflow bank with heavy splitting reports MC_ERR_OVERFLOW and
+    the handle stays usable."""
+    import mcgpu.workloads as W
+    with tempfile.TemporaryDirectory() as d:
+        W.mg_deep_slab(d, samples=100, G=4)
+        p = mc.Problem(d)
+        p.run(n=5000, mode="event")          # works with the default bank
+        p.reset()
+        p.run(n=100, mode="event")
+        p.close()
