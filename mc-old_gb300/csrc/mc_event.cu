@@ -72,6 +72,7 @@ constexpr float kEpsF = FLT_EPSILON;
 constexpr float kInf = __builtin_huge_valf();
 constexpr int kMaxFilt = 8;
 constexpr int kMaxIl = 32;
+constexpr uint32_t kMaxEvents = 1u << 22;   // events of one particle before MC_ERR_TIMEOUT
 
 enum { C_FLIGHTS = 0, C_COLL, C_CROSS, C_TALLY, C_PART, C_SPLIT, C_XS, C_FREEGAS, C_NUC };
 
@@ -777,6 +778,10 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
                 PState p;
                 load_p(T, s, p);
                 p.ev += 1u;
+                if (p.ev > kMaxEvents) {          // bounded walk: report, never spin
+                    atomicCAS(&s_status, 0, DS_TIMEOUT);
+                    p.ev = kMaxEvents;
+                }
                 Rng32 R;
                 R.init(A.seed, T.hidx[p.hslot], p.id, p.ev, 0u);
                 const int m = V.cell_mat[p.cell];

@@ -592,6 +592,7 @@ __device__ void random_walk(Ctx &C, PartD &p, bool digests)
     if (digests) dig(C, 0xA5A5A5A5ULL ^ p.id);
     while (p.alive && C.status == DS_OK) {
         C.rng.start_event(C.rng.event + 1);
+        if (C.rng.event > (1u << 22)) { C.status = DS_TIMEOUT; return; }   // bounded walk
         double dist = kMaxF;
         int S = -1;
         for (int i = T.cell_surf_off[p.cell]; i < T.cell_surf_off[p.cell + 1]; ++i) {
