@@ -456,6 +456,10 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
     const int s0 = V.est_score_off[e], ns = V.est_score_off[e + 1] - s0;
     const int *fac = V.est_factor + V.est_factor_off[e];
     const int base = V.est_bin_off[e];
+    if (!(fabsf(l_in) <= FLT_MAX)) {   // non-finite track: the loop below would never advance
+        atomicCAS(C.s_status, 0, DS_NAN);
+        return;
+    }
     Il il[kMaxIl];
     int off[kMaxFilt + 1], nil[kMaxFilt], idx[kMaxFilt];
     off[0] = 0;
@@ -467,7 +471,7 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
         off[i + 1] = off[i] + n;
         idx[i] = 0;
     }
-    for (;;) {
+    for (int guard = 0; guard <= off[nf]; ++guard) {   // each pass advances one filter
         float l = FLT_MAX;
         for (int i = 0; i < nf; ++i) { const float x = il[off[i] + idx[i]].l; l = (x < l) ? x : l; }
         int idx1 = 0;
@@ -537,19 +541,24 @@ __device__ __forceinline__ void scatter_direction(Rng32 &R, float dx, float dy, 
     float sa, ca;
     __sincosf(k2PiF * R.next(), &sa, &ca);
     const float Ac = sqrtf(fmaxf(1.f - mu0 * mu0, 0.f));
-    if (dz != 1.f) {
-        const float B = sqrtf(fmaxf(1.f - dz * dz, 0.f));
+    // the reference swaps to the y axis only for dz == 1 exactly; in FP32 a
+    // direction within 0.99 of +-z loses the formula's precision (and dz == -1
+    // divides by zero), so the swap covers both poles
+    if (fabsf(dz) < 0.99f) {
+        const float B = sqrtf(1.f - dz * dz);
         const float Cc = Ac / B;
         ox = dx * mu0 + (dx * dz * ca - dy * sa) * Cc;
         oy = dy * mu0 + (dy * dz * ca + dx * sa) * Cc;
         oz = dz * mu0 - ca * Ac * B;
     } else {
-        const float B = sqrtf(fmaxf(1.f - dy * dy, 0.f));
+        const float B = sqrtf(fmaxf(1.f - dy * dy, 1e-30f));
         const float Cc = Ac / B;
         ox = dx * mu0 + (dx * dy * ca - dz * sa) * Cc;
         oz = dz * mu0 + (dz * dy * ca + dx * sa) * Cc;
         oy = dy * mu0 - ca * Ac * B;
     }
+    const float r = rsqrtf(ox * ox + oy * oy + oz * oz);
+    ox *= r; oy *= r; oz *= r;
 }
 
 // Reaction.cpp:27-118 in FP32
@@ -875,6 +884,10 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
                     }
                     if (nuc >= 0 && !free_gas(C, R, p, __ldg(V.nuc_A + nuc))) atomicCAS(&s_status, 0, DS_TIMEOUT);
                 }
+            }
+            if (alive && !(fabsf(p.E) <= FLT_MAX && fabsf(p.u) <= 1.5f && fabsf(p.wt) <= FLT_MAX)) {
+                atomicCAS(&s_status, 0, DS_NAN);
+                alive = false;
             }
             if (alive) weight_roulette(C, R, p, alive);
             if (alive) {

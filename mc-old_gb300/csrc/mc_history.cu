@@ -362,6 +362,10 @@ __device__ void estimator_score(Ctx &C, int e, const PartD &p, double l_in)
     const int s0 = T.est_score_off[e], ns = T.est_score_off[e + 1] - s0;
     const double *fac = T.est_factor + T.est_factor_off[e];
     double *hist = C.hist + T.est_bin_off[e];
+    if (!(fabs(l_in) <= DBL_MAX)) {   // non-finite track: the loop below would never advance
+        C.status = DS_NAN;
+        return;
+    }
     Il il[kMaxIl];
     int off[kMaxFilt + 1], nil[kMaxFilt], idx[kMaxFilt];
     off[0] = 0;
@@ -373,7 +377,7 @@ __device__ void estimator_score(Ctx &C, int e, const PartD &p, double l_in)
         off[i + 1] = off[i] + n;
         idx[i] = 0;
     }
-    for (;;) {
+    for (int guard = 0; guard <= off[nf]; ++guard) {   // each pass advances one filter
         double l = kMaxF;
         for (int i = 0; i < nf; ++i) {
             const double x = il[off[i] + idx[i]].l;

@@ -449,6 +449,10 @@ static void estimator_score(orc_ctx *C, int e, const orc_particle *p, double l_i
     const int s0 = P->est_score_off[e], ns = P->est_score_off[e + 1] - s0;
     const double *fac = P->est_factor + P->est_factor_off[e];
     double *hist = C->hist + P->est_bin_off[e];
+    if (!(__builtin_fabs(l_in) <= DBL_MAX)) {   /* the loop below would never advance */
+        C->status = ORC_ERR_NAN;
+        return;
+    }
     orc_il il[ORC_MAX_IL];
     int off[ORC_MAX_FILT + 1], nil[ORC_MAX_FILT], idx[ORC_MAX_FILT];
     off[0] = 0;
@@ -460,7 +464,7 @@ static void estimator_score(orc_ctx *C, int e, const orc_particle *p, double l_i
         off[i + 1] = off[i] + n;
         idx[i] = 0;
     }
-    for (;;) {
+    for (int guard = 0; guard <= off[nf]; ++guard) {   /* each pass advances one filter */
         double l = ORC_MAX_F;
         for (int i = 0; i < nf; ++i) {          /* l = std::min(l, x) */
             const double x = il[off[i] + idx[i]].l;

@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-enum { ORC_OK = 0, ORC_ERR_INPUT = 1, ORC_ERR_OVERFLOW = 3, ORC_ERR_LOST = 4, ORC_ERR_NOMEM = 7 };
+enum { ORC_OK = 0, ORC_ERR_INPUT = 1, ORC_ERR_OVERFLOW = 3, ORC_ERR_LOST = 4, ORC_ERR_NAN = 6, ORC_ERR_NOMEM = 7 };
 
 /* surface types; coefficient layout (8 doubles per surface):
  *   PX/PY/PZ : [loc]
