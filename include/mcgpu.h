@@ -149,6 +149,25 @@ mc_status mc_histories_run(const mc_problem *p, uint64_t *n);
  * path, HDF5 not being available. */
 mc_status mc_report(const mc_problem *p, const char *path);
 
+/* FP64 replay of histories [first_history, first_history + n_histories)
+ * that allocates no device memory.  No counterpart in the reference: it is
+ * for callers that cannot allocate device memory once running (a host whose
+ * device memory belongs to another allocator's fixed pool, or a service that
+ * reserves everything at start-up).  The problem must already be loaded; the
+ * scratch (split stacks and per-history tally rows) lives in one fixed
+ * 64 MiB device array inside the library, held by every GPU that loads the
+ * library until the process exits.  Writes the per-bin sums of history
+ * totals and of their squares over the range to the caller's device arrays
+ * d_sum / d_sumsq (n_bins doubles each, all estimators in order, overwritten),
+ * equal bit for bit to what mc_run in MC_FP64_REPLAY adds for the same
+ * range; the handle's own tallies are not touched.  Problems with more tally
+ * bins than the scratch holds are refused with MC_ERR_ARG.  The first call on
+ * a device looks up the array's device address once; make that call before
+ * any stream capture.  Every call shares the one array, so calls that overlap
+ * on the GPU (two host threads, two handles) race; serialise them. */
+mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first_history, uint64_t n_histories,
+                                uint64_t seed, double *d_sum, double *d_sumsq);
+
 /* Human-readable message for the last failing call on p (never NULL). */
 const char *mc_last_error(const mc_problem *p);
 

@@ -40,6 +40,7 @@ SOURCES = [
     ("mc_evtables.cpp", "host"),
     ("mc_history.cu", "fp64"),
     ("mc_event.cu", "fast"),
+    ("mc_noalloc.cu", "fp64"),
 ]
 
 
