@@ -62,8 +62,10 @@ typedef struct {
     uint32_t grid_blocks;    /* blocks, 0 = fill the GPU */
     uint32_t stack_depth;    /* FP64 modes: split-particle stack per thread */
     uint32_t chunk;          /* FP64 modes: histories per fold chunk (0 = auto) */
-    uint32_t bank_capacity;  /* event mode: particles in flight (0 = auto) */
+    uint32_t bank_capacity;  /* event mode: particles per CTA tile (0 = tuned / 512) */
     uint32_t record_digests; /* FP64 modes: keep per-history event digests */
+    uint32_t blocks_per_sm;  /* event mode: 2, 3 or 4 resident CTAs per SM, which
+                                sets the register budget (0 = tuned / 4) */
 } mc_tune;
 
 /* Event counters and timing of the last mc_run.  The counts follow the
@@ -167,6 +169,39 @@ mc_status mc_report(const mc_problem *p, const char *path);
  * on the GPU (two host threads, two handles) race; serialise them. */
 mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first_history, uint64_t n_histories,
                                 uint64_t seed, double *d_sum, double *d_sumsq);
+
+/* Picks the event engine's launch shape (tile of particles per CTA and
+ * resident CTAs per SM) for this problem by timing sample_histories in each
+ * candidate shape; the winner becomes the handle's default for
+ * MC_MIXED_EVENT runs made with tune == NULL and is copied to *out.  The
+ * problem's tallies are left as they were.  No counterpart in the reference
+ * (it has no launch parameters). */
+mc_status mc_autotune(mc_problem *p, uint64_t sample_histories, uint64_t seed, mc_tune *out);
+
+/* ---- batches: many independent problems in one persistent launch ---------
+ * No counterpart in the reference, which runs one Simulator at a time.  A
+ * batch is a list of loaded problems with a history count each; mc_batch_run
+ * runs every history of every problem in ONE launch of the event engine
+ * (MC_MIXED_EVENT), replayed from a CUDA graph captured at the first run,
+ * and folds each problem's results into that problem's tallies (read them
+ * with mc_tally_read on the problem handles).  Problem i's histories use the
+ * seed  seed + 0x9E3779B97F4A7C15 * (i + 1),  so they are the histories an
+ * mc_run of that problem alone with that seed would follow.  The problems
+ * must outlive the batch and must not be run on their own while a batch run
+ * is in flight. */
+typedef struct mc_batch mc_batch;
+
+mc_status mc_batch_create(mc_problem *const *problems, uint32_t n, const uint64_t *histories,
+                          mc_batch **out);
+mc_status mc_batch_run(mc_batch *b, uint64_t seed, const mc_tune *tune);
+/* Counters and device time of the last mc_batch_run (summed over problems). */
+mc_status mc_batch_counters(const mc_batch *b, mc_counters *out);
+/* Times each candidate launch shape on the batch with every problem's
+ * histories scaled by sample_fraction (at least 64 each) and keeps the
+ * fastest for runs with tune == NULL; the problems' tallies are untouched. */
+mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double sample_fraction, mc_tune *out);
+mc_status mc_batch_free(mc_batch *b);
+const char *mc_batch_last_error(const mc_batch *b);
 
 /* Human-readable message for the last failing call on p (never NULL). */
 const char *mc_last_error(const mc_problem *p);

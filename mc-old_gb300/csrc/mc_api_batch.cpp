@@ -1,0 +1,194 @@
+// mc_api_batch.cpp -- autotuning and batches of problems (include/mcgpu.h).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mc_engine.h"
+#include "mc_handle.h"
+#include "mcgpu.h"
+
+using namespace mc;
+
+struct mc_batch {
+    BatchState *state = nullptr;
+    std::vector<mc_problem *> probs;
+    std::vector<uint64_t> hist;
+    mc_tune tuned{};
+    int sms = 0;
+    std::string err;
+};
+
+namespace {
+
+// Launch shapes the autotuners try: particles per CTA tile x CTAs per SM.
+struct Shape { uint32_t tile, minb; };
+const Shape kShapes[] = {{256, 4}, {512, 4}, {512, 3}, {1024, 3}, {512, 2}, {1024, 2}, {2048, 2}};
+
+}  // namespace
+
+extern "C" {
+
+mc_status mc_autotune(mc_problem *p, uint64_t sample, uint64_t seed, mc_tune *out)
+{
+    if (!p || !out) return MC_ERR_ARG;
+    if (!p->dev.ready) { p->err = "problem was not loaded"; return MC_ERR_ARG; }
+    if (sample == 0) sample = 200000;
+    DeviceProblem &d = p->dev;
+    const size_t nb = (size_t)std::max<long long>(d.dt.n_bins, 1);
+    double *tmp = nullptr;
+    if (cudaMalloc(&tmp, 2 * nb * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        p->err = "cannot allocate autotune tallies";
+        return MC_ERR_NOMEM;
+    }
+    double *keep_sum = d.d_sum, *keep_sq = d.d_sq;
+    const uint64_t keep_hist = d.histories, keep_ntrack = d.ntrack;
+    const mc_counters keep_last = d.last;
+    d.d_sum = tmp;
+    d.d_sq = tmp + nb;
+    std::string err;
+    mc_status st = MC_OK;
+    float best_ms = 1e30f;
+    mc_tune best{};
+    // one untimed run settles the event tables and scratch
+    mc_tune warm{};
+    warm.bank_capacity = 512;
+    warm.blocks_per_sm = 4;
+    st = run_event(p->t, d, 0, std::min<uint64_t>(sample, 20000), seed, &warm, err);
+    for (const Shape &sh : kShapes) {
+        if (st != MC_OK) break;
+        mc_tune t{};
+        t.bank_capacity = sh.tile;
+        t.blocks_per_sm = sh.minb;
+        std::string e2;
+        const mc_status s2 = run_event(p->t, d, 0, sample, seed, &t, e2);
+        if (s2 == MC_ERR_ARG) continue;            // shape does not fit (shared memory)
+        if (s2 != MC_OK) { st = s2; err = e2; break; }
+        if (d.last.transport_ms < best_ms) {
+            best_ms = (float)d.last.transport_ms;
+            best = t;
+        }
+    }
+    cudaStreamSynchronize(d.stream);
+    d.d_sum = keep_sum;
+    d.d_sq = keep_sq;
+    d.histories = keep_hist;
+    d.ntrack = keep_ntrack;
+    d.last = keep_last;
+    cudaFree(tmp);
+    if (st != MC_OK) { p->err = "autotune: " + err; return st; }
+    if (best.bank_capacity == 0) { p->err = "autotune: no launch shape fits"; return MC_ERR_ARG; }
+    d.tuned = best;
+    *out = best;
+    return MC_OK;
+}
+
+mc_status mc_batch_create(mc_problem *const *problems, uint32_t n, const uint64_t *histories, mc_batch **out)
+{
+    if (!problems || !histories || !out || n == 0) return MC_ERR_ARG;
+    *out = nullptr;
+    mc_batch *b = new mc_batch();
+    std::vector<const Tables *> tabs;
+    std::vector<DeviceProblem *> devs;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!problems[i] || !problems[i]->dev.ready) { delete b; return MC_ERR_ARG; }
+        tabs.push_back(&problems[i]->t);
+        devs.push_back(&problems[i]->dev);
+        b->probs.push_back(problems[i]);
+        b->hist.push_back(histories[i]);
+    }
+    b->sms = problems[0]->dev.sms;
+    mc_status st = batch_create(tabs, devs, histories, nullptr, &b->state, b->err);
+    *out = b;
+    return st;
+}
+
+mc_status mc_batch_run(mc_batch *b, uint64_t seed, const mc_tune *tune)
+{
+    if (!b || !b->state) return MC_ERR_ARG;
+    return batch_run(b->state, b->sms, seed, tune, b->tuned, b->err);
+}
+
+mc_status mc_batch_counters(const mc_batch *b, mc_counters *out)
+{
+    if (!b || !b->state || !out) return MC_ERR_ARG;
+    *out = batch_counters(b->state);
+    return MC_OK;
+}
+
+mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double frac, mc_tune *out)
+{
+    if (!b || !b->state || !out) return MC_ERR_ARG;
+    if (!(frac > 0.0) || frac > 1.0) frac = 0.02;
+    const uint32_t n = (uint32_t)b->probs.size();
+    std::vector<const Tables *> tabs;
+    std::vector<DeviceProblem *> devs;
+    std::vector<uint64_t> h(n);
+    size_t total_bins = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        tabs.push_back(&b->probs[i]->t);
+        devs.push_back(&b->probs[i]->dev);
+        h[i] = std::max<uint64_t>(64, (uint64_t)std::llround((double)b->hist[i] * frac));
+        total_bins += (size_t)std::max<long long>(b->probs[i]->dev.dt.n_bins, 1);
+    }
+    double *pool = nullptr;
+    if (cudaMalloc(&pool, 2 * total_bins * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        b->err = "cannot allocate autotune tallies";
+        return MC_ERR_NOMEM;
+    }
+    cudaMemset(pool, 0, 2 * total_bins * sizeof(double));
+    std::vector<double *> sums;
+    size_t off = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const size_t nb = (size_t)std::max<long long>(b->probs[i]->dev.dt.n_bins, 1);
+        sums.push_back(pool + off);
+        sums.push_back(pool + off + nb);
+        off += 2 * nb;
+    }
+    BatchState *trial = nullptr;
+    mc_status st = batch_create(tabs, devs, h.data(), &sums, &trial, b->err);
+    mc_tune best{};
+    float best_ms = 1e30f;
+    if (st == MC_OK) {
+        mc_tune none{};
+        st = batch_run(trial, b->sms, seed, nullptr, none, b->err);   // warm-up
+        for (const Shape &sh : kShapes) {
+            if (st != MC_OK) break;
+            mc_tune t{};
+            t.bank_capacity = sh.tile;
+            t.blocks_per_sm = sh.minb;
+            std::string e2;
+            const mc_status s2 = batch_run(trial, b->sms, seed, &t, none, e2);
+            if (s2 == MC_ERR_ARG) continue;
+            if (s2 != MC_OK) { st = s2; b->err = e2; break; }
+            const float ms = (float)batch_counters(trial).transport_ms;
+            if (ms < best_ms) { best_ms = ms; best = t; }
+        }
+    }
+    batch_state_free(trial);
+    cudaFree(pool);
+    if (st != MC_OK) return st;
+    if (best.bank_capacity == 0) { b->err = "autotune: no launch shape fits"; return MC_ERR_ARG; }
+    b->tuned = best;
+    *out = best;
+    return MC_OK;
+}
+
+mc_status mc_batch_free(mc_batch *b)
+{
+    if (!b) return MC_ERR_ARG;
+    batch_state_free(b->state);
+    delete b;
+    return MC_OK;
+}
+
+const char *mc_batch_last_error(const mc_batch *b)
+{
+    if (!b) return "null batch handle";
+    return b->err.c_str();
+}
+
+}  // extern "C"

@@ -20,6 +20,7 @@ struct DevBuf {
 };
 
 struct EventState;   // mixed-precision event engine (mc_event.cu)
+struct BatchState;   // batches of problems in one persistent launch (mc_event.cu)
 
 struct DeviceProblem {
     bool ready = false;
@@ -41,6 +42,7 @@ struct DeviceProblem {
     DevBuf hist, stack, digest, misc;
     // event engine (owned)
     EventState *ev_state = nullptr;
+    mc_tune tuned{};               // launch shape picked by mc_autotune (0 = defaults)
 };
 
 mc_status device_problem_init(const Tables &t, DeviceProblem &d, std::string &err);
@@ -62,6 +64,20 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
 mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n, uint64_t seed,
                     const mc_tune *tune, std::string &err);
 void event_state_free(EventState *s);
+bool event_tables_ready(const Tables &t, DeviceProblem &d, std::string &err);
+
+// batches (mc_event.cu)
+// sums_to (nullable): 2 device arrays per problem (sum, sumsq) to fold into
+// instead of the problems' own tallies (used while autotuning)
+mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vector<DeviceProblem *> &probs,
+                       const uint64_t *hist, const std::vector<double *> *sums_to, BatchState **out,
+                       std::string &err);
+cudaStream_t batch_stream(const BatchState *b);
+mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune *tune, const mc_tune &tuned,
+                    std::string &err);
+void batch_state_free(BatchState *b);
+const mc_counters &batch_counters(const BatchState *b);
+uint64_t batch_problem_seed(uint64_t seed, uint32_t i);
 
 mc_status status_from_device(int ds);
 std::string cuda_msg(cudaError_t e, const char *what);

@@ -33,7 +33,11 @@
 // Physics and tally semantics follow the reference line by line as the FP64
 // path does (see mc_history.cu); only the precision and the crossing logic
 // differ, so results agree statistically, not bit for bit.
+#include <algorithm>
 #include <cfloat>
+#include <cstring>
+#include <string>
+#include <vector>
 
 #include "mc_engine.h"
 #include "mc_evtables.h"
@@ -86,16 +90,25 @@ struct OvfP {
 struct EvArgs {
     uint64_t first, n, seed;
     unsigned long long *next;     // histories handed out (relative)
-    double *acc;                  // [grid * tile][nb]
+    double *acc;                  // [grid * tile][row_nb]
     unsigned long long *mask;     // [grid * tile][nw]
     int nw;
+    int row_nb;                   // bins per history row (largest problem)
     OvfP *ovf;                    // [grid][ovf_cap]
     int ovf_cap;
-    double *sum, *sq;             // global tallies
+    double *sum, *sq;             // global tallies (single problem)
     unsigned long long *counters;
     int *status;
     int tile;
     int smem_sums;                // per-CTA sums live in shared memory
+    // batch of problems (kBatch): history index space = concatenation of
+    // every problem's histories
+    const EvTables *tabs;         // [n_prob]
+    const unsigned long long *prefix;  // [n_prob + 1]
+    const unsigned long long *seeds;   // [n_prob]
+    double *const *psum;          // [n_prob] per-problem tallies
+    double *const *psq;
+    int n_prob;
 };
 
 // Philox stream of one particle and event, FP32 draws (4 per block)
@@ -129,17 +142,17 @@ struct Rng32 {
 // shared-memory tile (SoA) and per-CTA bookkeeping
 struct Tile {
     float *x, *y, *z, *u, *v, *w, *E, *wt, *t, *sig, *frac;
-    int *cell, *surf, *hs, *g, *gi, *sense;
+    int *cell, *surf, *hs, *g, *gi, *sense, *prob;
     uint32_t *id, *ev;
     unsigned short *qc, *qx;
     unsigned long long *hidx;
-    int *live, *hfree;
+    int *live, *hfree, *hprob;
     double *ssum, *ssq;
 };
 
 struct PState {
     float x, y, z, u, v, w, E, wt, t;
-    int cell, surf, hslot, g;
+    int cell, surf, hslot, g, prob;
     uint32_t id, ev;
 };
 
@@ -147,7 +160,7 @@ __device__ __forceinline__ void load_p(const Tile &T, int s, PState &p)
 {
     p.x = T.x[s]; p.y = T.y[s]; p.z = T.z[s]; p.u = T.u[s]; p.v = T.v[s]; p.w = T.w[s];
     p.E = T.E[s]; p.wt = T.wt[s]; p.t = T.t[s];
-    p.cell = T.cell[s]; p.surf = T.surf[s]; p.hslot = T.hs[s]; p.g = T.g[s];
+    p.cell = T.cell[s]; p.surf = T.surf[s]; p.hslot = T.hs[s]; p.g = T.g[s]; p.prob = T.prob[s];
     p.id = T.id[s]; p.ev = T.ev[s];
 }
 
@@ -155,12 +168,12 @@ __device__ __forceinline__ void store_p(const Tile &T, int s, const PState &p)
 {
     T.x[s] = p.x; T.y[s] = p.y; T.z[s] = p.z; T.u[s] = p.u; T.v[s] = p.v; T.w[s] = p.w;
     T.E[s] = p.E; T.wt[s] = p.wt; T.t[s] = p.t;
-    T.cell[s] = p.cell; T.surf[s] = p.surf; T.hs[s] = p.hslot; T.g[s] = p.g;
+    T.cell[s] = p.cell; T.surf[s] = p.surf; T.hs[s] = p.hslot; T.g[s] = p.g; T.prob[s] = p.prob;
     T.id[s] = p.id; T.ev[s] = p.ev;
 }
 
 struct Ctx {
-    const EvTables *V;
+    const EvTables *V;            // tables of the particle being processed
     const EvArgs *A;
     Tile T;
     unsigned long long cnt[kNumCounters];
@@ -168,7 +181,6 @@ struct Ctx {
     int *s_novf;
     int *s_nlive;
     int *s_nhfree;
-    int nb;
 };
 
 // ---------------------------------------------------------------------------
@@ -423,7 +435,7 @@ __device__ int filter_idx_l(const EvTables &V, int f, const PState &p, float t_o
 __device__ __forceinline__ void tally_add(Ctx &C, int hslot, int bin, double val)
 {
     const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
-    atomicAdd(C.A->acc + row * C.nb + bin, val);
+    atomicAdd(C.A->acc + row * C.A->row_nb + bin, val);
     unsigned long long *mw = C.A->mask + row * C.A->nw + (bin >> 6);
     const unsigned long long bit = 1ull << (bin & 63);
     if (!(*(volatile unsigned long long *)mw & bit)) atomicOr(mw, bit);
@@ -495,11 +507,19 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
 // ---------------------------------------------------------------------------
 // particle life cycle
 // ---------------------------------------------------------------------------
+// Folds a finished history's row into the sums (Estimator.cpp:339-346):
+// per-CTA shared sums for one problem, the problem's global sums in a batch.
 __device__ void history_fold(Ctx &C, int hslot)
 {
     const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
-    double *acc = C.A->acc + row * C.nb;
+    double *acc = C.A->acc + row * C.A->row_nb;
     unsigned long long *mask = C.A->mask + row * C.A->nw;
+    double *gs = C.A->sum, *gq = C.A->sq;
+    if (C.A->n_prob > 0) {
+        const int pr = C.T.hprob[hslot];
+        gs = C.A->psum[pr];
+        gq = C.A->psq[pr];
+    }
     for (int wi = 0; wi < C.A->nw; ++wi) {
         if (__ldcg(mask + wi) == 0ull) continue;
         unsigned long long m = atomicExch(mask + wi, 0ull);
@@ -513,8 +533,8 @@ __device__ void history_fold(Ctx &C, int hslot)
                 atomicAdd(C.T.ssum + bin, v);
                 atomicAdd(C.T.ssq + bin, v * v);
             } else {
-                atomicAdd(C.A->sum + bin, v);
-                atomicAdd(C.A->sq + bin, v * v);
+                atomicAdd(gs + bin, v);
+                atomicAdd(gq + bin, v * v);
             }
         }
     }
@@ -651,6 +671,7 @@ __device__ void sample_source(const EvTables &V, uint64_t seed, uint64_t hist, P
     p.g = V.src_group[s];
     p.id = 0u;
     p.ev = 0u;
+    p.prob = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -669,27 +690,43 @@ __device__ __forceinline__ int warp_append(int *counter, bool pred)
     return base + __popc(m & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
+// problem of a position in the concatenated history space of a batch
+__device__ __forceinline__ int problem_of(const EvArgs &A, unsigned long long gi)
+{
+    int lo = 0, hi = A.n_prob - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.prefix[mid] <= gi) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The persistent event loop.  MinB sets the register budget (MinB CTAs of
+// 256 threads resident per SM); kBatch runs many problems at once, each
+// particle resolving its own tables.
+template <int MinB, bool kBatch>
+__global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const EvArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const int P = A.tile;
     const int H = P;
-    // carve the tile
     Tile T;
     {
         unsigned char *q = smem;
         auto takef = [&](float *&ptr) { ptr = reinterpret_cast<float *>(q); q += sizeof(float) * P; };
         auto takei = [&](int *&ptr) { ptr = reinterpret_cast<int *>(q); q += sizeof(int) * P; };
+        const long long nsum = A.smem_sums ? V0.n_bins : 0;
         double *d = reinterpret_cast<double *>(q);
-        T.ssum = d; T.ssq = d + (A.smem_sums ? V.n_bins : 0);
-        q += sizeof(double) * (A.smem_sums ? 2 * V.n_bins : 0);
+        T.ssum = d; T.ssq = d + nsum;
+        q += sizeof(double) * 2 * nsum;
         T.hidx = reinterpret_cast<unsigned long long *>(q); q += sizeof(unsigned long long) * H;
         takef(T.x); takef(T.y); takef(T.z); takef(T.u); takef(T.v); takef(T.w);
         takef(T.E); takef(T.wt); takef(T.t); takef(T.sig); takef(T.frac);
-        takei(T.cell); takei(T.surf); takei(T.hs); takei(T.g); takei(T.gi); takei(T.sense);
+        takei(T.cell); takei(T.surf); takei(T.hs); takei(T.g); takei(T.gi); takei(T.sense); takei(T.prob);
         T.id = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
         T.ev = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
-        takei(T.live); takei(T.hfree);
+        takei(T.live); takei(T.hfree); takei(T.hprob);
         T.qc = reinterpret_cast<unsigned short *>(q); q += sizeof(unsigned short) * P;
         T.qx = reinterpret_cast<unsigned short *>(q); q += sizeof(unsigned short) * P;
     }
@@ -698,15 +735,16 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
     __shared__ unsigned long long s_hist_base;
 
     Ctx C;
-    C.V = &V;
+    C.V = &V0;
     C.A = &A;
     C.T = T;
     C.s_status = &s_status;
     C.s_novf = &s_novf;
     C.s_nlive = &s_nlive;
     C.s_nhfree = &s_nhfree;
-    C.nb = (int)V.n_bins;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
+    auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
+    auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
 
     for (int s = threadIdx.x; s < P; s += blockDim.x) {
         T.hs[s] = -1;
@@ -714,7 +752,7 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
         T.live[s] = 0;
     }
     if (A.smem_sums)
-        for (int b = threadIdx.x; b < 2 * V.n_bins; b += blockDim.x) T.ssum[b] = 0.0;
+        for (int b = threadIdx.x; b < 2 * V0.n_bins; b += blockDim.x) T.ssum[b] = 0.0;
     if (threadIdx.x == 0) {
         s_nlive = 0; s_novf = 0; s_nhfree = H; s_status = 0; s_nqc = 0; s_nqx = 0;
         s_exhausted = 0;
@@ -730,7 +768,7 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
             s_take_ovf = take;
             s_ovf_base = s_novf - take;
             s_novf -= take;
-            int need = free_slots - take;
+            const int need = free_slots - take;
             int got = 0;
             if (need > 0 && s_novf == 0 && !s_exhausted && s_status == 0) {
                 const unsigned long long g0 = atomicAdd(A.next, (unsigned long long)need);
@@ -762,16 +800,25 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
                 p.x = o.x; p.y = o.y; p.z = o.z; p.u = o.u; p.v = o.v; p.w = o.w;
                 p.E = o.E; p.wt = o.wt; p.t = o.t; p.cell = o.cell; p.surf = o.surf;
                 p.hslot = o.hslot; p.g = o.g; p.id = o.id; p.ev = 0u;
+                p.prob = T.hprob[o.hslot];
                 store_p(T, s, p);
                 C.cnt[C_PART]++;
             } else if (r - s_take_ovf < s_got) {
                 const int k = r - s_take_ovf;
                 const int hslot = T.hfree[s_hfree_base + k];
-                const uint64_t hist = A.first + s_hist_base + (uint64_t)k;
+                const unsigned long long gi = s_hist_base + (unsigned long long)k;
+                int prob = 0;
+                uint64_t hist = A.first + gi;
+                if (kBatch) {
+                    prob = problem_of(A, gi);
+                    hist = gi - A.prefix[prob];
+                }
                 T.hidx[hslot] = hist;
+                T.hprob[hslot] = prob;
                 T.live[hslot] = 1;
-                sample_source(V, A.seed, hist, p);
+                sample_source(tab(prob), seed_of(prob), hist, p);
                 p.hslot = hslot;
+                p.prob = prob;
                 store_p(T, s, p);
                 C.cnt[C_PART]++;
             }
@@ -786,13 +833,15 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
             if (live) {
                 PState p;
                 load_p(T, s, p);
+                const EvTables &V = tab(p.prob);
+                C.V = &V;
                 p.ev += 1u;
                 if (p.ev > kMaxEvents) {          // bounded walk: report, never spin
                     atomicCAS(&s_status, 0, DS_TIMEOUT);
                     p.ev = kMaxEvents;
                 }
                 Rng32 R;
-                R.init(A.seed, T.hidx[p.hslot], p.id, p.ev, 0u);
+                R.init(seed_of(p.prob), T.hidx[p.hslot], p.id, p.ev, 0u);
                 const int m = V.cell_mat[p.cell];
                 float sig = 0.f, dcol;
                 if (m >= 0) {
@@ -811,10 +860,13 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
                 const bool cross = dcol > dist;
                 const float l = cross ? dist : dcol;
                 if (!cross || S >= 0) {
-                    const float speed = speed_of(p.E);
                     const float t_old = p.t;
                     p.x = fmaf(p.u, l, p.x); p.y = fmaf(p.v, l, p.y); p.z = fmaf(p.w, l, p.z);
-                    if (V.has_time) p.t = t_old + l / speed;
+                    float speed = 0.f;
+                    if (V.has_time) {
+                        speed = speed_of(p.E);
+                        p.t = t_old + l / speed;
+                    }
                     C.cnt[C_FLIGHTS]++;
                     if (m >= 0 && V.G == 0) C.cnt[C_NUC] += (unsigned long long)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
                     for (int i = V.cell_tl_off[p.cell]; i < V.cell_tl_off[p.cell + 1]; ++i)
@@ -842,8 +894,10 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
             const int s = T.qc[j];
             PState p;
             load_p(T, s, p);
+            const EvTables &V = tab(p.prob);
+            C.V = &V;
             Rng32 R;
-            R.init(A.seed, T.hidx[p.hslot], p.id, p.ev, 1u);
+            R.init(seed_of(p.prob), T.hidx[p.hslot], p.id, p.ev, 1u);
             C.cnt[C_COLL]++;
             bool alive = true;
             const int m = V.cell_mat[p.cell];
@@ -851,7 +905,7 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
                 alive = false;
             } else {
                 for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
-                    estimator_score(C, V.cell_c[i], p, p.t, speed_of(p.E), 0.f);
+                    estimator_score(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f);
                 const float st = T.sig[s];
                 if (V.G > 0) {
                     const int row = m * V.G + p.g;
@@ -890,11 +944,8 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
                 alive = false;
             }
             if (alive) weight_roulette(C, R, p, alive);
-            if (alive) {
-                store_p(T, s, p);
-            } else {
-                particle_dies(C, s, p.hslot);
-            }
+            if (alive) store_p(T, s, p);
+            else particle_dies(C, s, p.hslot);
         }
 
         // ---------------- cross ----------------
@@ -903,8 +954,10 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
             const int s = T.qx[j];
             PState p;
             load_p(T, s, p);
+            const EvTables &V = tab(p.prob);
+            C.V = &V;
             Rng32 R;
-            R.init(A.seed, T.hidx[p.hslot], p.id, p.ev, 1u);
+            R.init(seed_of(p.prob), T.hidx[p.hslot], p.id, p.ev, 1u);
             C.cnt[C_CROSS]++;
             const int S = T.gi[s];
             const int old_cell = p.cell;
@@ -923,7 +976,7 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
                 surface_reflect(V, S, p);
             }
             if (p.wt != 0.f) {   // a vacuum boundary kills first and scores zero (general.cpp:98-111)
-                const float speed = speed_of(p.E);
+                const float speed = V.has_time ? speed_of(p.E) : 0.f;
                 for (int i = V.surf_est_off[S]; i < V.surf_est_off[S + 1]; ++i)
                     estimator_score(C, V.surf_est[i], p, p.t, speed, 0.f);
             }
@@ -969,7 +1022,7 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
     // flush per-CTA sums and counters
     __syncthreads();
     if (A.smem_sums) {
-        for (int b = threadIdx.x; b < V.n_bins; b += blockDim.x) {
+        for (int b = threadIdx.x; b < V0.n_bins; b += blockDim.x) {
             const double sv = T.ssum[b], qv = T.ssq[b];
             if (sv != 0.0) atomicAdd(A.sum + b, sv);
             if (qv != 0.0) atomicAdd(A.sq + b, qv);
@@ -983,75 +1036,147 @@ __global__ void __launch_bounds__(256) k_event(const EvTables V, const EvArgs A)
     }
 }
 
-size_t tile_smem_bytes(int P, long long nb, bool smem_sums)
+size_t tile_smem_bytes(int P, long long nb_smem)
 {
     size_t b = 0;
-    b += smem_sums ? sizeof(double) * 2 * (size_t)nb : 0;
+    b += sizeof(double) * 2 * (size_t)nb_smem;
     b += sizeof(unsigned long long) * P;
     b += 11 * sizeof(float) * P;
-    b += 6 * sizeof(int) * P;
+    b += 7 * sizeof(int) * P;
     b += 2 * sizeof(uint32_t) * P;
-    b += 2 * sizeof(int) * P;
+    b += 3 * sizeof(int) * P;
     b += 2 * sizeof(unsigned short) * P;
     return b + 64;
 }
 
+typedef void (*EvKernel)(const EvTables, const EvArgs);
+
+EvKernel pick_kernel(int minb, bool batch)
+{
+    if (batch) {
+        switch (minb) {
+        case 2: return k_event<2, true>;
+        case 3: return k_event<3, true>;
+        default: return k_event<4, true>;
+        }
+    }
+    switch (minb) {
+    case 2: return k_event<2, false>;
+    case 3: return k_event<3, false>;
+    default: return k_event<4, false>;
+    }
+}
+
 }  // namespace
 
-mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n, uint64_t seed,
-                    const mc_tune *tune, std::string &err)
+bool event_tables_ready(const Tables &t, DeviceProblem &d, std::string &err)
 {
+    if (d.ev_state) return true;
+    EventState *S = new EventState();
+    if (!build_event_tables(t, S->host, err)) { delete S; return false; }
     cudaError_t e;
-    if (!d.ev_state) {
-        EventState *S = new EventState();
-        if (!build_event_tables(t, S->host, err)) { delete S; return MC_ERR_INPUT; }
-        if ((e = cudaMalloc(&S->d_blob, S->host.blob.size())) != cudaSuccess) {
-            delete S;
-            err = cuda_msg(e, "cudaMalloc(event tables)");
-            return MC_ERR_NOMEM;
-        }
-        cudaMemcpy(S->d_blob, S->host.blob.data(), S->host.blob.size(), cudaMemcpyHostToDevice);
-        S->dv = S->host.view;
-        for (auto &f : S->host.fix) *f.first = static_cast<const char *>(S->d_blob) + f.second;
-        S->dv = S->host.view;
-        d.ev_state = S;
+    if ((e = cudaMalloc(&S->d_blob, S->host.blob.size())) != cudaSuccess) {
+        delete S;
+        err = cuda_msg(e, "cudaMalloc(event tables)");
+        return false;
     }
-    EventState &S = *d.ev_state;
-    const EvTables &V = S.dv;
-    const int block = (tune && tune->block) ? (int)tune->block : 256;
-    if (block != 256) { err = "the event kernel is built for 256-thread blocks"; return MC_ERR_ARG; }
-    int tile = (tune && tune->bank_capacity) ? (int)tune->bank_capacity : 512;
-    if (tile < block || tile % block != 0 || tile > 4096) { err = "tile (bank_capacity) must be a multiple of 256 up to 4096"; return MC_ERR_ARG; }
-    const long long nb = std::max<long long>(V.n_bins, 1);
-    const bool smem_sums = nb <= 4096;
-    const size_t smem = tile_smem_bytes(tile, nb, smem_sums);
-    if ((e = cudaFuncSetAttribute(k_event, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) {
+    cudaMemcpy(S->d_blob, S->host.blob.data(), S->host.blob.size(), cudaMemcpyHostToDevice);
+    for (auto &f : S->host.fix) *f.first = static_cast<const char *>(S->d_blob) + f.second;
+    S->dv = S->host.view;
+    d.ev_state = S;
+    return true;
+}
+
+const EvTables &event_tables_view(const DeviceProblem &d) { return d.ev_state->dv; }
+
+// Launch geometry of the event kernel for a tune (0 fields = tuned / defaults).
+struct EvLaunch {
+    int block = 256, tile = 512, minb = 4, grid = 0;
+    size_t smem = 0;
+};
+
+static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune, const mc_tune &tuned,
+                                    long long nb_smem, bool batch, EvLaunch &L, std::string &err)
+{
+    L.block = (tune && tune->block) ? (int)tune->block : 256;
+    if (L.block != 256) { err = "the event kernel is built for 256-thread blocks"; return MC_ERR_ARG; }
+    L.tile = (tune && tune->bank_capacity) ? (int)tune->bank_capacity
+           : (tuned.bank_capacity ? (int)tuned.bank_capacity : 512);
+    if (L.tile < L.block || L.tile % L.block != 0 || L.tile > 4096) {
+        err = "tile (bank_capacity) must be a multiple of 256 up to 4096";
+        return MC_ERR_ARG;
+    }
+    L.minb = (tune && tune->blocks_per_sm) ? (int)tune->blocks_per_sm
+           : (tuned.blocks_per_sm ? (int)tuned.blocks_per_sm : 4);
+    if (L.minb < 2 || L.minb > 4) { err = "blocks_per_sm must be 2, 3 or 4"; return MC_ERR_ARG; }
+    L.smem = tile_smem_bytes(L.tile, nb_smem);
+    EvKernel k = pick_kernel(L.minb, batch);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem)) != cudaSuccess) {
         err = cuda_msg(e, "event kernel shared memory");
         return MC_ERR_ARG;
     }
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_event, block, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, L.block, L.smem);
     if (per_sm < 1) { err = "event kernel does not fit on an SM with this tile"; return MC_ERR_ARG; }
-    int grid = (tune && tune->grid_blocks) ? (int)tune->grid_blocks : d.sms * per_sm;
-    const int nw = (int)((nb + 63) / 64);
-    const int ovf_cap = 4 * tile;
+    per_sm = std::min(per_sm, L.minb);
+    L.grid = (tune && tune->grid_blocks) ? (int)tune->grid_blocks : d.sms * per_sm;
+    return MC_OK;
+}
+
+static mc_status event_scratch(EventState &S, cudaStream_t st, int grid, int tile, long long row_nb,
+                               std::string &err)
+{
+    const int nw = (int)((row_nb + 63) / 64);
     const size_t rows = (size_t)grid * tile;
-    const bool grow = !S.acc.ptr || S.acc.bytes < rows * nb * sizeof(double);
-    if (!devbuf_reserve(S.acc, rows * nb * sizeof(double)) ||
-        !devbuf_reserve(S.mask, rows * nw * sizeof(unsigned long long)) ||
-        !devbuf_reserve(S.ovf, (size_t)grid * ovf_cap * sizeof(OvfP)) ||
+    const size_t acc_bytes = rows * row_nb * sizeof(double);
+    const size_t mask_bytes = rows * nw * sizeof(unsigned long long);
+    const bool grow = !S.acc.ptr || S.acc.bytes < acc_bytes || S.mask.bytes < mask_bytes;
+    if (!devbuf_reserve(S.acc, acc_bytes) || !devbuf_reserve(S.mask, mask_bytes) ||
+        !devbuf_reserve(S.ovf, (size_t)grid * 4 * tile * sizeof(OvfP)) ||
         !devbuf_reserve(S.misc, 256 + kNumCounters * sizeof(unsigned long long))) {
         err = "cannot allocate event-engine scratch";
         return MC_ERR_NOMEM;
     }
     if (grow || S.rows_dirty) {
-        cudaMemsetAsync(S.acc.ptr, 0, rows * nb * sizeof(double), d.stream);
-        cudaMemsetAsync(S.mask.ptr, 0, rows * nw * sizeof(unsigned long long), d.stream);
+        cudaMemsetAsync(S.acc.ptr, 0, S.acc.bytes, st);
+        cudaMemsetAsync(S.mask.ptr, 0, S.mask.bytes, st);
         S.rows_dirty = false;
     }
+    return MC_OK;
+}
+
+static const char *status_text(int hs)
+{
+    return hs == DS_LOST ? "a particle was lost (no cell contains it)"
+         : hs == DS_OVERFLOW ? "split-particle bank or time-filter buffer overflow"
+         : hs == DS_TIMEOUT ? "a particle exceeded the event limit or the free-gas loop did not converge"
+         : hs == DS_NAN ? "a non-finite track length, energy or weight" : "device error status";
+}
+
+static void fill_counters(mc_counters &L, const unsigned long long *cnt)
+{
+    L.flights = cnt[0]; L.collisions = cnt[1]; L.crossings = cnt[2]; L.tally_updates = cnt[3];
+    L.particles = cnt[4]; L.splits = cnt[5]; L.xs_evals = cnt[6]; L.freegas_iters = cnt[7];
+    L.nuc_lookups = cnt[8];
+}
+
+mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n, uint64_t seed,
+                    const mc_tune *tune, std::string &err)
+{
+    if (!event_tables_ready(t, d, err)) return MC_ERR_INPUT;
+    EventState &S = *d.ev_state;
+    const EvTables &V = S.dv;
+    const long long nb = std::max<long long>(V.n_bins, 1);
+    const bool smem_sums = nb <= 4096;
+    EvLaunch L;
+    mc_status st = event_launch_shape(d, tune, d.tuned, smem_sums ? nb : 0, false, L, err);
+    if (st != MC_OK) return st;
+    const int ovf_cap = 4 * L.tile;
+    if ((st = event_scratch(S, d.stream, L.grid, L.tile, nb, err)) != MC_OK) return st;
     char *misc = static_cast<char *>(S.misc.ptr);
     cudaMemsetAsync(misc, 0, 256 + kNumCounters * sizeof(unsigned long long), d.stream);
-    EvArgs A;
+    EvArgs A{};
     A.first = first;
     A.n = n;
     A.seed = seed;
@@ -1060,15 +1185,18 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     A.counters = reinterpret_cast<unsigned long long *>(misc + 64);
     A.acc = static_cast<double *>(S.acc.ptr);
     A.mask = static_cast<unsigned long long *>(S.mask.ptr);
-    A.nw = nw;
+    A.nw = (int)((nb + 63) / 64);
+    A.row_nb = (int)nb;
     A.ovf = static_cast<OvfP *>(S.ovf.ptr);
     A.ovf_cap = ovf_cap;
     A.sum = d.d_sum;
     A.sq = d.d_sq;
-    A.tile = tile;
+    A.tile = L.tile;
     A.smem_sums = smem_sums ? 1 : 0;
+    A.n_prob = 0;
     cudaEventRecord(d.ev[0], d.stream);
-    k_event<<<grid, block, smem, d.stream>>>(V, A);
+    pick_kernel(L.minb, false)<<<L.grid, L.block, L.smem, d.stream>>>(V, A);
+    cudaError_t e;
     if ((e = cudaGetLastError()) != cudaSuccess) { err = cuda_msg(e, "event kernel launch"); return MC_ERR_CUDA; }
     cudaEventRecord(d.ev[1], d.stream);
     int hs = 0;
@@ -1084,23 +1212,210 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     cudaEventElapsedTime(&ms, d.ev[0], d.ev[1]);
     if (hs != DS_OK) {
         S.rows_dirty = true;
-        err = hs == DS_LOST ? "a particle was lost (no cell contains it)"
-            : hs == DS_OVERFLOW ? "split-particle bank or time-filter buffer overflow"
-            : hs == DS_TIMEOUT ? "free-gas rejection loop did not converge" : "device error status";
+        err = status_text(hs);
         return status_from_device(hs);
     }
-    mc_counters &L = d.last;
-    L.flights = cnt[0]; L.collisions = cnt[1]; L.crossings = cnt[2]; L.tally_updates = cnt[3];
-    L.particles = cnt[4]; L.splits = cnt[5]; L.xs_evals = cnt[6]; L.freegas_iters = cnt[7];
-    L.nuc_lookups = cnt[8];
-    L.histories = n;
-    L.transport_ms = ms;
-    L.fold_ms = 0.0;
-    L.total_ms = ms;
-    L.launches = 1;
+    mc_counters &C = d.last;
+    fill_counters(C, cnt);
+    C.histories = n;
+    C.transport_ms = ms;
+    C.total_ms = ms;
+    C.launches = 1;
     d.histories += n;
-    d.ntrack += L.flights;
+    d.ntrack += C.flights;
     return MC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// batches of problems in one persistent launch, replayed from a CUDA graph
+// ---------------------------------------------------------------------------
+struct BatchState {
+    std::vector<DeviceProblem *> probs;
+    std::vector<uint64_t> hist;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    DevBuf meta;                      // tabs, prefix, seeds, psum, psq
+    EventState scratch;               // rows / mask / overflow / control
+    long long row_nb = 1;
+    uint64_t total = 0;
+    unsigned long long *h_seeds = nullptr;   // pinned: per-problem seeds of the next run
+    cudaGraphExec_t exec = nullptr;
+    EvLaunch shape;
+    bool have_shape = false;
+    bool count_histories = true;      // false for autotuning batches
+    mc_counters last{};
+};
+
+void batch_state_free(BatchState *b)
+{
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    devbuf_free(b->meta);
+    devbuf_free(b->scratch.acc);
+    devbuf_free(b->scratch.mask);
+    devbuf_free(b->scratch.ovf);
+    devbuf_free(b->scratch.misc);
+    if (b->h_seeds) cudaFreeHost(b->h_seeds);
+    for (auto &e : b->ev) if (e) cudaEventDestroy(e);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+uint64_t batch_problem_seed(uint64_t seed, uint32_t i) { return seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1); }
+
+mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vector<DeviceProblem *> &probs,
+                       const uint64_t *hist, const std::vector<double *> *sums_to, BatchState **out,
+                       std::string &err)
+{
+    BatchState *b = new BatchState();
+    b->probs = probs;
+    const uint32_t n = (uint32_t)probs.size();
+    std::vector<EvTables> views(n);
+    std::vector<unsigned long long> prefix(n + 1, 0);
+    std::vector<double *> psum(n), psq(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!event_tables_ready(*tabs[i], *probs[i], err)) { batch_state_free(b); err = "problem " + std::to_string(i) + ": " + err; return MC_ERR_INPUT; }
+        views[i] = probs[i]->ev_state->dv;
+        prefix[i + 1] = prefix[i] + hist[i];
+        b->hist.push_back(hist[i]);
+        psum[i] = sums_to ? (*sums_to)[2 * i] : probs[i]->d_sum;
+        psq[i] = sums_to ? (*sums_to)[2 * i + 1] : probs[i]->d_sq;
+        b->row_nb = std::max<long long>(b->row_nb, views[i].n_bins);
+    }
+    b->total = prefix[n];
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        batch_state_free(b);
+        err = cuda_msg(e, "batch stream");
+        return MC_ERR_CUDA;
+    }
+    for (auto &ev : b->ev) cudaEventCreate(&ev);
+    const size_t sz = n * sizeof(EvTables) + (n + 1) * 8 + n * 8 + 2 * n * sizeof(double *) + 6 * 256;
+    if (!devbuf_reserve(b->meta, sz) || cudaHostAlloc(&b->h_seeds, n * 8, cudaHostAllocDefault) != cudaSuccess) {
+        batch_state_free(b);
+        err = "cannot allocate batch descriptors";
+        return MC_ERR_NOMEM;
+    }
+    char *m = static_cast<char *>(b->meta.ptr);
+    size_t off = 0;
+    auto put = [&](const void *src, size_t bytes) {
+        off = (off + 255) & ~(size_t)255;
+        cudaMemcpy(m + off, src, bytes, cudaMemcpyHostToDevice);
+        const size_t at = off;
+        off += bytes;
+        return at;
+    };
+    put(views.data(), n * sizeof(EvTables));
+    put(prefix.data(), (n + 1) * 8);
+    put(psum.data(), n * sizeof(double *));
+    put(psq.data(), n * sizeof(double *));
+    b->count_histories = sums_to == nullptr;
+    *out = b;
+    return MC_OK;
+}
+
+mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune *tune, const mc_tune &tuned,
+                    std::string &err)
+{
+    const uint32_t n = (uint32_t)b->probs.size();
+    DeviceProblem shape_dev;
+    shape_dev.sms = device_sms;
+    EvLaunch L;
+    mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, L, err);
+    if (st != MC_OK) return st;
+    if ((st = event_scratch(b->scratch, b->stream, L.grid, L.tile, b->row_nb, err)) != MC_OK) return st;
+    const bool same_shape = b->have_shape && L.grid == b->shape.grid && L.tile == b->shape.tile &&
+                            L.minb == b->shape.minb;
+    for (uint32_t i = 0; i < n; ++i) b->h_seeds[i] = batch_problem_seed(seed, i);
+    char *m = static_cast<char *>(b->meta.ptr);
+    size_t off = 0;
+    auto at = [&](size_t bytes) { off = (off + 255) & ~(size_t)255; const size_t a = off; off += bytes; return m + a; };
+    const EvTables *d_tabs = reinterpret_cast<const EvTables *>(at(n * sizeof(EvTables)));
+    const unsigned long long *d_prefix = reinterpret_cast<const unsigned long long *>(at((n + 1) * 8));
+    double *const *d_psum = reinterpret_cast<double *const *>(at(n * sizeof(double *)));
+    double *const *d_psq = reinterpret_cast<double *const *>(at(n * sizeof(double *)));
+    unsigned long long *d_seeds = reinterpret_cast<unsigned long long *>(at(n * 8));
+    cudaError_t e;
+    if (!same_shape) {
+        if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+        char *misc = static_cast<char *>(b->scratch.misc.ptr);
+        EvArgs A{};
+        A.first = 0;
+        A.n = b->total;
+        A.seed = 0;
+        A.next = reinterpret_cast<unsigned long long *>(misc);
+        A.status = reinterpret_cast<int *>(misc + 8);
+        A.counters = reinterpret_cast<unsigned long long *>(misc + 64);
+        A.acc = static_cast<double *>(b->scratch.acc.ptr);
+        A.mask = static_cast<unsigned long long *>(b->scratch.mask.ptr);
+        A.nw = (int)((b->row_nb + 63) / 64);
+        A.row_nb = (int)b->row_nb;
+        A.ovf = static_cast<OvfP *>(b->scratch.ovf.ptr);
+        A.ovf_cap = 4 * L.tile;
+        A.tile = L.tile;
+        A.smem_sums = 0;
+        A.tabs = d_tabs;
+        A.prefix = d_prefix;
+        A.seeds = d_seeds;
+        A.psum = d_psum;
+        A.psq = d_psq;
+        A.n_prob = (int)n;
+        EvTables V0{};
+        V0.n_bins = 0;
+        // capture: seeds (pinned host -> device), control reset, the launch
+        cudaGraph_t g = nullptr;
+        if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+            err = cuda_msg(e, "graph capture");
+            return MC_ERR_CUDA;
+        }
+        cudaMemcpyAsync(d_seeds, b->h_seeds, n * 8, cudaMemcpyHostToDevice, b->stream);
+        cudaMemsetAsync(misc, 0, 256 + kNumCounters * sizeof(unsigned long long), b->stream);
+        pick_kernel(L.minb, true)<<<L.grid, L.block, L.smem, b->stream>>>(V0, A);
+        if ((e = cudaStreamEndCapture(b->stream, &g)) != cudaSuccess) {
+            err = cuda_msg(e, "graph capture end");
+            return MC_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { err = cuda_msg(e, "graph instantiate"); return MC_ERR_CUDA; }
+        b->shape = L;
+        b->have_shape = true;
+    }
+    cudaEventRecord(b->ev[0], b->stream);
+    if ((e = cudaGraphLaunch(b->exec, b->stream)) != cudaSuccess) { err = cuda_msg(e, "graph launch"); return MC_ERR_CUDA; }
+    cudaEventRecord(b->ev[1], b->stream);
+    char *misc = static_cast<char *>(b->scratch.misc.ptr);
+    int hs = 0;
+    unsigned long long cnt[kNumCounters];
+    if ((e = cudaMemcpyAsync(&hs, misc + 8, sizeof(int), cudaMemcpyDeviceToHost, b->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(cnt, misc + 64, sizeof(cnt), cudaMemcpyDeviceToHost, b->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(b->stream)) != cudaSuccess) {
+        err = cuda_msg(e, "batch kernel");
+        b->scratch.rows_dirty = true;
+        return MC_ERR_CUDA;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]);
+    if (hs != DS_OK) {
+        b->scratch.rows_dirty = true;
+        b->have_shape = false;    // re-capture: the row memset must run first
+        err = status_text(hs);
+        return status_from_device(hs);
+    }
+    std::memset(&b->last, 0, sizeof(b->last));
+    fill_counters(b->last, cnt);
+    b->last.histories = b->total;
+    b->last.transport_ms = ms;
+    b->last.total_ms = ms;
+    b->last.launches = 1;
+    if (b->count_histories)
+        for (uint32_t i = 0; i < n; ++i) b->probs[i]->histories += b->hist[i];
+    return MC_OK;
+}
+
+cudaStream_t batch_stream(const BatchState *b) { return b->stream; }
+
+const mc_counters &batch_counters(const BatchState *b) { return b->last; }
 
 }  // namespace mc

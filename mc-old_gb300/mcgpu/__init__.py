@@ -45,7 +45,8 @@ class InputError(McError):
 class Tune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("grid_blocks", ctypes.c_uint32),
                 ("stack_depth", ctypes.c_uint32), ("chunk", ctypes.c_uint32),
-                ("bank_capacity", ctypes.c_uint32), ("record_digests", ctypes.c_uint32)]
+                ("bank_capacity", ctypes.c_uint32), ("record_digests", ctypes.c_uint32),
+                ("blocks_per_sm", ctypes.c_uint32)]
 
 
 class Counters(ctypes.Structure):
@@ -88,6 +89,14 @@ def lib() -> ctypes.CDLL:
         L.mc_nsample.argtypes = [P, ctypes.POINTER(u64)]
         L.mc_histories_run.argtypes = [P, ctypes.POINTER(u64)]
         L.mc_report.argtypes = [P, ctypes.c_char_p]
+        L.mc_autotune.argtypes = [P, u64, u64, ctypes.POINTER(Tune)]
+        L.mc_batch_create.argtypes = [ctypes.POINTER(P), u32, ctypes.POINTER(u64), ctypes.POINTER(P)]
+        L.mc_batch_run.argtypes = [P, u64, ctypes.POINTER(Tune)]
+        L.mc_batch_counters.argtypes = [P, ctypes.POINTER(Counters)]
+        L.mc_batch_autotune.argtypes = [P, u64, ctypes.c_double, ctypes.POINTER(Tune)]
+        L.mc_batch_free.argtypes = [P]
+        L.mc_batch_last_error.argtypes = [P]
+        L.mc_batch_last_error.restype = ctypes.c_char_p
         L.mc_last_error.argtypes = [P]
         L.mc_last_error.restype = ctypes.c_char_p
         L.mc_status_string.argtypes = [st]
@@ -96,7 +105,8 @@ def lib() -> ctypes.CDLL:
                   "mc_problem_table_bytes", "mc_run", "mc_reset_tallies",
                   "mc_tally_count", "mc_tally_size", "mc_estimator_name", "mc_tally_read",
                   "mc_counters_read", "mc_digests_read", "mc_nsample", "mc_histories_run",
-                  "mc_report"):
+                  "mc_report", "mc_autotune", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
+                  "mc_batch_autotune", "mc_batch_free"):
             getattr(L, f).restype = st
         _lib = L
     return _lib
@@ -206,6 +216,65 @@ class Problem:
 
     def report(self, path: str):
         self._check(lib().mc_report(self._h, os.fsencode(path)))
+
+    def autotune(self, sample: int = 200000, seed: int = DEFAULT_SEED) -> dict:
+        """Pick and keep the event engine's fastest launch shape."""
+        t = Tune()
+        self._check(lib().mc_autotune(self._h, sample, seed, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+
+def batch_problem_seed(seed: int, i: int) -> int:
+    """Seed of problem i inside a batch run with `seed` (include/mcgpu.h)."""
+    return (seed + 0x9E3779B97F4A7C15 * (i + 1)) & 0xFFFFFFFFFFFFFFFF
+
+
+class Batch:
+    """Many loaded problems run together in one persistent launch."""
+
+    def __init__(self, problems, histories):
+        L = lib()
+        self.problems = list(problems)
+        arr = (ctypes.c_void_p * len(self.problems))(*[p._h.value for p in self.problems])
+        hist = (ctypes.c_uint64 * len(self.problems))(*[int(h) for h in histories])
+        self.histories = [int(h) for h in histories]
+        self._h = ctypes.c_void_p()
+        st = L.mc_batch_create(arr, len(self.problems), hist, ctypes.byref(self._h))
+        if st != 0:
+            msg = L.mc_batch_last_error(self._h).decode() if self._h else "batch create failed"
+            self.close()
+            raise McError(st, msg)
+
+    def _check(self, st):
+        if st != 0:
+            raise McError(st, lib().mc_batch_last_error(self._h).decode())
+
+    def run(self, seed: int = DEFAULT_SEED, tune: Tune | None = None, **tune_kw) -> dict:
+        if tune is None and tune_kw:
+            tune = make_tune(**tune_kw)
+        self._check(lib().mc_batch_run(self._h, seed, ctypes.byref(tune) if tune is not None else None))
+        return self.counters()
+
+    def counters(self) -> dict:
+        c = Counters()
+        self._check(lib().mc_batch_counters(self._h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def autotune(self, seed: int = DEFAULT_SEED, fraction: float = 0.02) -> dict:
+        t = Tune()
+        self._check(lib().mc_batch_autotune(self._h, seed, fraction, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().mc_batch_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 @dataclass

@@ -24,6 +24,9 @@ Workloads (sizes are the defaults; all can be shrunk for tests):
                      weight roulette 0.25 -> 1.0, importance 2^r.
   mg_layered_slab    16 x 1 cm single-group regions (the differentiation
                      workload).
+  batch_shields      4096 independent multigroup slab or sphere shields of
+                     uneven size (1-8 regions, 1 or 8 groups, 1-50 mean free
+                     paths, 10^3-10^6 histories each, log-uniform).
 """
 from __future__ import annotations
 
@@ -285,3 +288,74 @@ def mg_layered_slab(out_dir: str, samples: int = 10_000_000, n_regions: int = 16
            "    </estimator>\n")
     return _mg_slab_xml(out_dir, "mg_layered_slab", samples, [1.0] * n_regions, tot, sca,
                         [1.0] * n_regions, est)
+
+
+def _log_uniform_int(rng: np.random.Generator, lo: float, hi: float) -> int:
+    """round(exp(U(ln lo, ln hi))) with the exponential in decimal."""
+    u = rng.uniform(0.0, 1.0)
+    ctx = decimal.Context(prec=40)
+    a = ctx.ln(decimal.Decimal(repr(lo)))
+    b = ctx.ln(decimal.Decimal(repr(hi)))
+    x = ctx.exp(ctx.add(a, ctx.multiply(ctx.subtract(b, a), decimal.Decimal(repr(u)))))
+    return int(x.to_integral_value(rounding=decimal.ROUND_HALF_EVEN))
+
+
+def _mg_sphere_xml(out_dir, name, samples, radii, tot, sca, estimators):
+    R, G = tot.shape
+    s = [_xml_header(name, samples)]
+    s.append(f"<multigroup groups=\"{G}\"/>\n<materials>\n")
+    for r in range(R):
+        s.append(f"    <material name=\"m{r}\">\n        <multigroup total=\""
+                 + " ".join(_fmt(v) for v in tot[r]) + "\"\n            scatter=\""
+                 + " ".join(_fmt(v) for v in sca[r].reshape(-1)) + "\"/>\n    </material>\n")
+    s.append("</materials>\n<surfaces>\n")
+    for i, rad in enumerate(radii):
+        s.append(f"    <sphere name=\"s{i}\" x=\"0\" y=\"0\" z=\"0\" r=\"{_fmt(rad)}\"/>\n")
+    s.append("</surfaces>\n<cells>\n")
+    for r in range(R):
+        s.append(f"    <cell name=\"c{r}\" material=\"m{r}\">\n")
+        if r > 0:
+            s.append(f"        <surface name=\"s{r - 1}\" sense=\"+1\"/>\n")
+        s.append(f"        <surface name=\"s{r}\" sense=\"-1\"/>\n    </cell>\n")
+    s.append(f"    <cell name=\"outside\" importance=\"0.0\">\n        <surface name=\"s{R - 1}\" sense=\"+1\"/>\n"
+             "    </cell>\n</cells>\n")
+    s.append("<sources>\n    <point x=\"0\" y=\"0\" z=\"0\" group=\"0\"/>\n</sources>\n")
+    s.append("<estimators>\n" + estimators.replace("@R", str(R - 1)) + "</estimators>\n")
+    os.makedirs(out_dir, exist_ok=True)
+    with open(os.path.join(out_dir, "input.xml"), "w") as f:
+        f.write("".join(s))
+    return out_dir
+
+
+def batch_shields(root: str, n_problems: int = 4096, min_hist: float = 1e3, max_hist: float = 1e6, k: int = 4):
+    """Writes n_problems shield inputs under root/p0000, ... and returns
+    [(dir, histories), ...].  Each problem: slab or sphere (p = 1/2), R ~
+    U{1..8} regions of equal width, total thickness T ~ U[1, 50] mean free
+    paths of the first region's group 1, G = 1 or 8 (p = 1/2), sigma_t,g ~
+    U[0.2, 2], scatter ratio ~ U[0.5, 0.95] split downward by Dirichlet(1);
+    histories log-uniform on [min_hist, max_hist].  Tally: leakage (slab:
+    transmission and reflection) with a group filter."""
+    rng = _rng(k)
+    out = []
+    for i in range(n_problems):
+        d = os.path.join(root, f"p{i:04d}")
+        sphere = rng.uniform() < 0.5
+        R = int(rng.integers(1, 9))
+        G = 1 if rng.uniform() < 0.5 else 8
+        T = rng.uniform(1.0, 50.0)
+        tot, sca = mg_slab_data(R, G, k, rng=rng)
+        width = T / tot[0, 0] / R
+        n = _log_uniform_int(rng, min_hist, max_hist)
+        if sphere:
+            radii = [width * (r + 1) for r in range(R)]
+            est = ("    <estimator name=\"leakage\" scores=\"cross\">\n        <surface name=\"s@R\"/>\n"
+                   "        <filter type=\"group\"/>\n    </estimator>\n")
+            _mg_sphere_xml(d, f"sphere{i}", n, radii, tot, sca, est)
+        else:
+            est = ("    <estimator name=\"leakage\" scores=\"cross\">\n        <surface name=\"p@R\"/>\n"
+                   "        <filter type=\"group\"/>\n    </estimator>\n"
+                   "    <estimator name=\"reflected\" scores=\"cross\">\n        <surface name=\"p0\"/>\n"
+                   "    </estimator>\n")
+            _mg_slab_xml(d, f"slab{i}", n, [width] * R, tot, sca, [1.0] * R, est)
+        out.append((d, n))
+    return out

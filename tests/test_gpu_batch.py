@@ -1,0 +1,113 @@
+"""Batches of independent problems in one persistent launch (CUDA graph) and
+the launch-shape autotuners."""
+import tempfile
+
+import numpy as np
+import pytest
+
+from stats import assert_agree
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mc():
+    import build as B
+    B.build()
+    import mcgpu
+    return mcgpu
+
+
+def _problems(mc, root, n, lo=2000, hi=20000):
+    import mcgpu.workloads as W
+    specs = W.batch_shields(root, n_problems=n, min_hist=lo, max_hist=hi)
+    return [mc.Problem(d) for d, _ in specs], [h for _, h in specs]
+
+
+def test_batch_equals_problems_run_alone(mc):
+    """Problem i of a batch follows the histories of a lone run with seed
+    batch_problem_seed(seed, i): same answers (summation order aside)."""
+    seed = 777
+    with tempfile.TemporaryDirectory() as root:
+        probs, hist = _problems(mc, root, 24)
+        b = mc.Batch(probs, hist)
+        c = b.run(seed=seed)
+        assert c["histories"] == sum(hist)
+        assert c["launches"] == 1
+        batch_res = [p.all_tallies() for p in probs]
+        for i, p in enumerate(probs):
+            assert p.histories_run() == hist[i]
+        b.close()
+        for i, (d_p, n) in enumerate(zip(probs, hist)):
+            d_p.reset()
+            d_p.run(n=n, seed=mc.batch_problem_seed(seed, i), mode="event")
+            m1, s1, su1, _ = batch_res[i]
+            m2, s2, su2, _ = d_p.all_tallies()
+            assert np.allclose(su1, su2, rtol=1e-6, atol=1e-12), f"problem {i}"
+            assert_agree(m1, s1, m2, s2, f"problem {i}")
+        for p in probs:
+            p.close()
+
+
+def test_batch_agrees_with_fp64(mc):
+    with tempfile.TemporaryDirectory() as root:
+        probs, hist = _problems(mc, root, 16)
+        b = mc.Batch(probs, hist)
+        b.run(seed=5)
+        ev = [p.all_tallies() for p in probs]
+        b.close()
+        for i, p in enumerate(probs):
+            p.reset()
+            p.run(n=hist[i], seed=99, mode="replay")
+            m2, s2, _, _ = p.all_tallies()
+            assert_agree(ev[i][0], ev[i][1], m2, s2, f"problem {i}")
+            p.close()
+
+
+def test_batch_graph_replays_with_new_seeds(mc):
+    with tempfile.TemporaryDirectory() as root:
+        probs, hist = _problems(mc, root, 12)
+        b = mc.Batch(probs, hist)
+        b.run(seed=1)
+        first = [p.all_tallies()[2].copy() for p in probs]
+        for p in probs:
+            p.reset()
+        b.run(seed=2)                 # replays the captured graph
+        second = [p.all_tallies()[2].copy() for p in probs]
+        for p in probs:
+            p.reset()
+        b.run(seed=1)
+        again = [p.all_tallies()[2].copy() for p in probs]
+        b.close()
+        assert any(not np.allclose(a, c) for a, c in zip(first, second))
+        for a, c in zip(first, again):
+            assert np.allclose(a, c, rtol=1e-9, atol=1e-12)
+        for p in probs:
+            p.close()
+
+
+def test_autotune_single_and_batch(mc):
+    import cases
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case("ce_sphere_small", d)
+        p = mc.Problem(d, d + "/xs_library")
+        p.run(n=1000, mode="event")
+        before = p.all_tallies()[2].copy()
+        t = p.autotune(sample=20000)
+        assert t["bank_capacity"] in (256, 512, 1024, 2048) and t["blocks_per_sm"] in (2, 3, 4)
+        assert np.array_equal(p.all_tallies()[2], before)       # tallies untouched
+        assert p.histories_run() == 1000
+        p.run(n=1000, first=1000, mode="event")                 # uses the tuned shape
+        assert p.histories_run() == 2000
+        p.close()
+    with tempfile.TemporaryDirectory() as root:
+        probs, hist = _problems(mc, root, 8)
+        b = mc.Batch(probs, hist)
+        t = b.autotune(fraction=0.05)
+        assert t["bank_capacity"] > 0
+        assert all(p.histories_run() == 0 for p in probs)
+        b.run(seed=3)
+        assert all(p.histories_run() == h for p, h in zip(probs, hist))
+        b.close()
+        for p in probs:
+            p.close()
