@@ -220,10 +220,13 @@ def gpu_arm(a):
     import numpy as np
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    if a.workload == "batch":
+        return batch_arm(a, mcgpu, torch, flush, rank, world, dist)
     with tempfile.TemporaryDirectory() as tmp:
         d = make_workload(tmp, a.histories)
         prob = mcgpu.Problem(d, os.path.join(d, "xs_library"))
         H = a.histories
+        tuned = prob.autotune(sample=min(H, 1_000_000), seed=SEED + 17) if a.mode == "event" else None
         base = rank * (a.steps + a.warmup + a.e2e_steps + 1) * H
         for w in range(a.warmup):
             prob.reset()
@@ -305,6 +308,8 @@ def gpu_arm(a):
         "dtype": {"event": "f32 tracking / f64 tallies", "plain": "f64", "replay": "f64"}[a.mode],
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "histories_per_step": H, "mode": a.mode,
+                   "launch_shape": ({"tile": tuned["bank_capacity"], "blocks_per_sm": tuned["blocks_per_sm"]}
+                                    if tuned else None),
                    "l2": "flushed (256 MiB write) before every timed step; XS tables L2-resident by design",
                    "parallelism": f"dp{world} (disjoint history ranges)"},
         "fom": {"value": statistics.mean(fom) if fom else None, "unit": "1/s",
@@ -328,13 +333,70 @@ def gpu_arm(a):
     return 0
 
 
+def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
+    """Config of 4096 uneven multigroup shields in one persistent launch."""
+    from mcgpu import workloads as W
+    import numpy as np
+    with tempfile.TemporaryDirectory() as tmp:
+        specs = W.batch_shields(tmp, n_problems=a.batch_problems)
+        probs = [mcgpu.Problem(d) for d, _ in specs]
+        hist = [h for _, h in specs]
+        b = mcgpu.Batch(probs, hist)
+        tuned = b.autotune(seed=SEED + 17, fraction=0.01)
+        for w in range(a.warmup):
+            for p in probs:
+                p.reset()
+            b.run(seed=SEED + 1000 + w)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+        sampler.start()
+        ms, launches, foms = 0.0, 0, []
+        for k in range(a.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            for p in probs:
+                p.reset()
+            c = b.run(seed=SEED + k)
+            ms += c["total_ms"]
+            launches += c["launches"]
+        clocks = sampler.stop()
+        T = ms / a.steps * 1e-3
+        for p in probs:
+            m, s, _, _ = p.tally(0)
+            tot = float(np.sum(m))
+            if tot > 0:
+                err = float(np.sqrt(np.sum(s ** 2))) / tot
+                foms.append(1.0 / (err * err * T))
+        b.close()
+        for p in probs:
+            p.close()
+    total = sum(hist)
+    line = {"metric": METRIC, "value": total / T, "unit": "histories/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": T * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 tracking / f64 tallies", "data": "synthetic",
+            "config": {"workload": f"batch_shields: {len(hist)} MG slab/sphere shields, {total} histories, "
+                                   "one persistent launch from a CUDA graph",
+                       "launch_shape": {"tile": tuned["bank_capacity"], "blocks_per_sm": tuned["blocks_per_sm"]},
+                       "l2": "flushed (256 MiB write) before every timed step"},
+            "batch_latency_ms": T * 1e3,
+            "fom_per_problem": {"median": float(np.median(foms)), "min": float(np.min(foms)),
+                                "max": float(np.max(foms)), "unit": "1/s",
+                                "tally": "total leakage, R over the group bins, T = whole-batch latency"},
+            "clocks": clocks, "gpu_launches": launches}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="plain", choices=["event", "plain", "replay"])
+    ap.add_argument("--mode", default="event", choices=["event", "plain", "replay"])
+    ap.add_argument("--workload", default="ce_sphere", choices=["ce_sphere", "batch"])
+    ap.add_argument("--batch-problems", type=int, default=4096)
     ap.add_argument("--histories", type=int, default=10_000_000)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-histories", type=int, default=4000)
