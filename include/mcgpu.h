@@ -178,6 +178,29 @@ mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first_history, uint64_t 
  * (it has no launch parameters). */
 mc_status mc_autotune(mc_problem *p, uint64_t sample_histories, uint64_t seed, mc_tune *out);
 
+/* ---- tally derivatives (one-group multigroup problems) -------------------
+ * No counterpart in the reference.  The parameters are every material's
+ * one-group (Sigma_s, Sigma_a) in input order: params[2m], params[2m+1]
+ * (1/cm for a material written with <multigroup>).  Both calls run FP64
+ * replay histories [0, n) keyed by seed and leave the problem's own tallies
+ * untouched; runs at different parameters with the same (n, seed) use common
+ * random numbers. */
+
+/* The problem's own parameters (2 per material). */
+mc_status mc_lr_params(const mc_problem *p, double *params, uint32_t cap);
+
+/* Every tally bin (all estimators in order) at the given parameters: mean and
+ * standard error (either pointer may be NULL). */
+mc_status mc_forward(mc_problem *p, const double *params, uint64_t n_histories, uint64_t seed,
+                     double *tally_out, double *sigma_out);
+
+/* d(tally bin b)/d(param k) at the given parameters by the likelihood-ratio
+ * (differential-operator) kernel, dtally[b * n_params + k], with its
+ * standard error in sigma (nullable).  n_params = 2 x materials.  Density
+ * derivatives follow as d/d rho_m = Sigma_s,m d/dSigma_s,m + Sigma_a,m d/dSigma_a,m. */
+mc_status mc_backward(mc_problem *p, const double *params, uint64_t n_histories, uint64_t seed,
+                      double *dtally, double *sigma);
+
 /* ---- batches: many independent problems in one persistent launch ---------
  * No counterpart in the reference, which runs one Simulator at a time.  A
  * batch is a list of loaded problems with a history count each; mc_batch_run

@@ -39,6 +39,7 @@ SOURCES = [
     ("mc_report.cpp", "host"),
     ("mc_evtables.cpp", "host"),
     ("mc_api_batch.cpp", "host"),
+    ("mc_lr.cpp", "host"),
     ("mc_history.cu", "fp64"),
     ("mc_event.cu", "fast"),
     ("mc_noalloc.cu", "fp64"),

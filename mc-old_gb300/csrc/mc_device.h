@@ -58,7 +58,14 @@ struct HistoryArgs {
     unsigned long long *digest;     // [n] or nullptr
     int *status;
     unsigned int *next;      // work counter (zeroed by the launcher)
+    // likelihood-ratio differentiation (n_params > 0): each history row is
+    // followed by n_bins x n_params derivative contributions; split copies
+    // keep their score-function weights in lr_stack
+    int n_params = 0;
+    double *lr_stack = nullptr;   // [threads][stack_depth][n_params]
 };
+
+constexpr int kMaxLrParams = 64;   // (Sigma_s, Sigma_a) for up to 32 materials
 
 // FP64 history-based transport of one chunk.  replay selects the portable
 // elementary functions (bit-exact with the CPU oracle); otherwise CUDA's

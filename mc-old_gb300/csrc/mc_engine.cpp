@@ -143,6 +143,8 @@ void device_problem_free(DeviceProblem &d)
     if (d.stream) cudaStreamSynchronize(d.stream);
     event_state_free(d.ev_state);
     d.ev_state = nullptr;
+    lr_scratch_free(d.lr);
+    d.lr = nullptr;
     devbuf_free(d.hist); devbuf_free(d.stack); devbuf_free(d.digest); devbuf_free(d.misc);
     if (d.blob) cudaFree(d.blob);
     if (d.h_blob) cudaFreeHost(d.h_blob);

@@ -43,6 +43,7 @@ struct DeviceProblem {
     // event engine (owned)
     EventState *ev_state = nullptr;
     mc_tune tuned{};               // launch shape picked by mc_autotune (0 = defaults)
+    void *lr = nullptr;            // forward / backward scratch (mc_lr.cpp)
 };
 
 mc_status device_problem_init(const Tables &t, DeviceProblem &d, std::string &err);
@@ -80,6 +81,7 @@ const mc_counters &batch_counters(const BatchState *b);
 uint64_t batch_problem_seed(uint64_t seed, uint32_t i);
 
 mc_status status_from_device(int ds);
+void lr_scratch_free(void *lr);
 std::string cuda_msg(cudaError_t e, const char *what);
 
 }  // namespace mc

@@ -36,6 +36,7 @@ constexpr double kMaxF = (double)FLT_MAX;
 constexpr double kMaxFLess = 0.9 * kMaxF;
 constexpr int kMaxFilt = 8;
 constexpr int kMaxIl = 64;
+constexpr int kMaxParams = kMaxLrParams;
 
 enum { C_FLIGHTS = 0, C_COLL, C_CROSS, C_TALLY, C_PART, C_SPLIT, C_XS, C_FREEGAS, C_NUC };
 
@@ -69,6 +70,13 @@ struct Ctx {
     int depth;
     int sp;
     int status;
+    // likelihood-ratio (differentiation) state, used only by the L kernels:
+    // S[k] = d ln(weight x path probability) / d param_k of the particle being
+    // walked; split copies keep theirs in lr_stack
+    double S[kMaxParams];
+    double *lr_stack;
+    int K;                 // parameters: (Sigma_s, Sigma_a) per material
+    long long nb;          // bins; the derivative rows follow the tally row
 };
 
 __device__ __forceinline__ void dig(Ctx &C, unsigned long long v)
@@ -354,7 +362,26 @@ __device__ double score_value(Ctx &C, int sc, const PartD &p, double l)
     }
 }
 
+// d(score)/d(Sigma_s), d(score)/d(Sigma_a) of the cell's material when the
+// score itself holds a cross section (Estimator.cpp:29, 60-124); 1-group
+__device__ __forceinline__ void direct_terms(const Ctx &C, int sc, int m, const PartD &p, double v,
+                                             double &ds, double &da)
+{
+    const DevTables &T = *C.T;
+    ds = 0.0;
+    da = 0.0;
+    if (m < 0) return;
+    const int i = m * T.mg_groups + p.g;
+    const double st = T.mg_total[i], ss = T.mg_scat_tot[i], sa = T.mg_capture[i];
+    const int kind = T.score_kind[sc];
+    if (kind == 2 && ss != 0.0) ds += v / ss;
+    if ((kind == 1 || kind == 3) && sa != 0.0) da += v / sa;
+    if (kind == 4) { ds += v / st; da += v / st; }
+    if (T.score_kernel[sc] == 1) { ds -= v / st; da -= v / st; }
+}
+
 // Estimator::score (Estimator.cpp:298-336)
+template <bool L>
 __device__ void estimator_score(Ctx &C, int e, const PartD &p, double l_in)
 {
     const DevTables &T = *C.T;
@@ -386,8 +413,22 @@ __device__ void estimator_score(Ctx &C, int e, const PartD &p, double l_in)
         int idx1 = 0;
         for (int i = 0; i < nf; ++i) idx1 += (int)(il[off[i] + idx[i]].bin * fac[i + 1]);
         for (int s = 0; s < ns; ++s) {
-            hist[idx1] += score_value(C, s0 + s, p, l);
+            const double v = score_value(C, s0 + s, p, l);
+            hist[idx1] += v;
             C.cnt[C_TALLY]++;
+            if constexpr (L) {
+                // d(contribution)/d(param_k) = v S_k + direct dependence
+                double *dh = C.hist + C.nb + (size_t)(T.est_bin_off[e] + idx1) * C.K;
+                double ds, da;
+                direct_terms(C, s0 + s, T.cell_mat[p.cell], p, v, ds, da);
+                const int m = T.cell_mat[p.cell];
+                for (int k = 0; k < C.K; ++k) {
+                    double d = v * C.S[k];
+                    if (m >= 0 && k == 2 * m) d += ds;
+                    if (m >= 0 && k == 2 * m + 1) d += da;
+                    dh[k] += d;
+                }
+            }
             idx1 += (int)fac[0];
         }
         for (int i = 0; i < nf; ++i) {
@@ -413,6 +454,7 @@ __device__ __forceinline__ void weight_roulette(Ctx &C, PartD &p)
 }
 
 // population_control.cpp:21-49
+template <bool L>
 __device__ void cell_importance(Ctx &C, PartD &p)
 {
     const DevTables &T = *C.T;
@@ -430,6 +472,8 @@ __device__ void cell_importance(Ctx &C, PartD &p)
             if (C.sp >= C.depth) { C.status = DS_OVERFLOW; return; }
             PartD q = p;
             q.id = child_id(p.id, C.rng.event, (uint32_t)(i + 1));
+            if constexpr (L)
+                for (int k = 0; k < C.K; ++k) C.lr_stack[(size_t)C.sp * C.K + k] = C.S[k];
             C.stack[C.sp++] = q;
             C.cnt[C_SPLIT]++;
         }
@@ -450,6 +494,7 @@ __device__ int search_cell(const DevTables &T, double px, double py, double pz)
 }
 
 // general.cpp:73-83
+template <bool L>
 __device__ void move_particle(Ctx &C, PartD &p, double l)
 {
     const DevTables &T = *C.T;
@@ -457,11 +502,16 @@ __device__ void move_particle(Ctx &C, PartD &p, double l)
     C.cnt[C_FLIGHTS]++;
     const int m = T.cell_mat[p.cell];
     if (m >= 0 && T.mg_groups == 0) C.cnt[C_NUC] += (unsigned long long)(T.mat_off[m + 1] - T.mat_off[m]);
+    if constexpr (L) {
+        // the flight's probability carries exp(-Sigma_t l): d/dSigma_s = d/dSigma_a = -l
+        if (m >= 0) { C.S[2 * m] -= l; C.S[2 * m + 1] -= l; }
+    }
     for (int i = T.cell_tl_off[p.cell]; i < T.cell_tl_off[p.cell + 1]; ++i)
-        estimator_score(C, T.cell_tl[i], p, l);
+        estimator_score<L>(C, T.cell_tl[i], p, l);
 }
 
 // general.cpp:89-115
+template <bool L>
 __device__ void surface_hit(Ctx &C, PartD &p, int s)
 {
     const DevTables &T = *C.T;
@@ -483,8 +533,8 @@ __device__ void surface_hit(Ctx &C, PartD &p, int s)
         p.cell_old = p.cell;
     }
     for (int i = T.surf_est_off[s]; i < T.surf_est_off[s + 1]; ++i)
-        estimator_score(C, T.surf_est[i], p, 0.0);
-    cell_importance(C, p);
+        estimator_score<L>(C, T.surf_est[i], p, 0.0);
+    cell_importance<L>(C, p);
 }
 
 // Reaction.cpp:27-118
@@ -535,7 +585,7 @@ __device__ void free_gas_scatter(Ctx &C, PartD &p, double A)
 }
 
 // general.cpp:121-163 without implicit fission
-template <bool R>
+template <bool R, bool L>
 __device__ void collision(Ctx &C, PartD &p)
 {
     const DevTables &T = *C.T;
@@ -543,7 +593,12 @@ __device__ void collision(Ctx &C, PartD &p)
     const int m = T.cell_mat[p.cell];
     if (m < 0) { p_kill(p); return; }
     for (int i = T.cell_c_off[p.cell]; i < T.cell_c_off[p.cell + 1]; ++i)
-        estimator_score(C, T.cell_c[i], p, 0.0);
+        estimator_score<L>(C, T.cell_c[i], p, 0.0);
+    if constexpr (L) {
+        // collision density Sigma_t times implicit-capture factor Sigma_s/Sigma_t
+        // = Sigma_s: d/dSigma_s = 1/Sigma_s, d/dSigma_a = 0 (1 group)
+        C.S[2 * m] += 1.0 / T.mg_scat_tot[m * T.mg_groups + p.g];
+    }
     const double implicit = macro_xs(C, m, XS_C, p) + 0.0;
     p.wgt = p.wgt * (macro_xs(C, m, XS_T, p) - implicit) / macro_xs(C, m, XS_T, p);
     if (T.mg_groups > 0) {
@@ -586,7 +641,7 @@ __device__ void digest_event(Ctx &C, const PartD &p, unsigned long long type)
 }
 
 // general.cpp:177-211
-template <bool R>
+template <bool R, bool L>
 __device__ void random_walk(Ctx &C, PartD &p, bool digests)
 {
     const DevTables &T = *C.T;
@@ -608,12 +663,12 @@ __device__ void random_walk(Ctx &C, PartD &p, bool digests)
         unsigned long long type;
         if (dcol > dist) {
             if (S < 0) { C.status = DS_LOST; return; }
-            move_particle(C, p, dist);
-            surface_hit(C, p, S);
+            move_particle<L>(C, p, dist);
+            surface_hit<L>(C, p, S);
             type = 1;
         } else {
-            move_particle(C, p, dcol);
-            collision<R>(C, p);
+            move_particle<L>(C, p, dcol);
+            collision<R, L>(C, p);
             type = 2;
         }
         weight_roulette(C, p);
@@ -663,34 +718,43 @@ __device__ void sample_source(Ctx &C, PartD &p)
     p.id = 0;
 }
 
-template <bool R>
+template <bool R, bool L>
 __global__ void __launch_bounds__(128) k_history_fp64(const DevTables T, const HistoryArgs A)
 {
     Ctx C;
     C.T = &T;
     C.depth = (int)A.stack_depth;
-    C.stack = reinterpret_cast<PartD *>(A.stack) +
-              (size_t)(blockIdx.x * blockDim.x + threadIdx.x) * A.stack_depth;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    C.stack = reinterpret_cast<PartD *>(A.stack) + tid * A.stack_depth;
     C.status = DS_OK;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
     const long long nb = T.n_bins;
+    C.nb = nb;
+    C.K = L ? A.n_params : 0;
+    C.lr_stack = L ? A.lr_stack + tid * A.stack_depth * (size_t)A.n_params : nullptr;
+    const long long row = L ? nb * (1 + (long long)A.n_params) : nb;
     const bool digests = A.digest != nullptr;
     for (;;) {
         const unsigned hl = atomicAdd(A.next, 1u);
         if (hl >= A.n) break;
         const uint64_t h = A.first + hl;
-        C.hist = A.hist + (size_t)hl * nb;
-        for (long long b = 0; b < nb; ++b) C.hist[b] = 0.0;
+        C.hist = A.hist + (size_t)hl * row;
+        for (long long b = 0; b < row; ++b) C.hist[b] = 0.0;
         C.rng.init(A.seed, h);
         C.digest = 0xCBF29CE484222325ULL;
         PartD p;
         p.E_old = 0.0;
         sample_source<R>(C, p);
         C.sp = 0;
+        if constexpr (L)
+            for (int k = 0; k < C.K; ++k) C.lr_stack[k] = 0.0;
         C.stack[C.sp++] = p;
         while (C.sp > 0 && C.status == DS_OK) {
-            PartD q = C.stack[--C.sp];
-            random_walk<R>(C, q, digests);
+            --C.sp;
+            PartD q = C.stack[C.sp];
+            if constexpr (L)
+                for (int k = 0; k < C.K; ++k) C.S[k] = C.lr_stack[(size_t)C.sp * C.K + k];
+            random_walk<R, L>(C, q, digests);
         }
         if (digests) A.digest[hl] = C.digest;
         if (C.status != DS_OK) {
@@ -756,8 +820,8 @@ int history_fp64_max_threads(bool replay, int block)
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (replay) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_history_fp64<true>, block, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_history_fp64<false>, block, 0);
+    if (replay) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_history_fp64<true, false>, block, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_history_fp64<false, false>, block, 0);
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm * block;
 }
@@ -765,8 +829,14 @@ int history_fp64_max_threads(bool replay, int block)
 cudaError_t launch_history_fp64(const DevTables &T, const HistoryArgs &A, bool replay, int grid, int block,
                                 cudaStream_t st)
 {
-    if (replay) k_history_fp64<true><<<grid, block, 0, st>>>(T, A);
-    else k_history_fp64<false><<<grid, block, 0, st>>>(T, A);
+    if (A.n_params > 0) {
+        if (!replay || A.n_params > kMaxParams) return cudaErrorInvalidValue;
+        k_history_fp64<true, true><<<grid, block, 0, st>>>(T, A);
+    } else if (replay) {
+        k_history_fp64<true, false><<<grid, block, 0, st>>>(T, A);
+    } else {
+        k_history_fp64<false, false><<<grid, block, 0, st>>>(T, A);
+    }
     return cudaGetLastError();
 }
 

@@ -90,6 +90,9 @@ def lib() -> ctypes.CDLL:
         L.mc_histories_run.argtypes = [P, ctypes.POINTER(u64)]
         L.mc_report.argtypes = [P, ctypes.c_char_p]
         L.mc_autotune.argtypes = [P, u64, u64, ctypes.POINTER(Tune)]
+        L.mc_lr_params.argtypes = [P, P, u32]
+        L.mc_forward.argtypes = [P, P, u64, u64, P, P]
+        L.mc_backward.argtypes = [P, P, u64, u64, P, P]
         L.mc_batch_create.argtypes = [ctypes.POINTER(P), u32, ctypes.POINTER(u64), ctypes.POINTER(P)]
         L.mc_batch_run.argtypes = [P, u64, ctypes.POINTER(Tune)]
         L.mc_batch_counters.argtypes = [P, ctypes.POINTER(Counters)]
@@ -105,7 +108,7 @@ def lib() -> ctypes.CDLL:
                   "mc_problem_table_bytes", "mc_run", "mc_reset_tallies",
                   "mc_tally_count", "mc_tally_size", "mc_estimator_name", "mc_tally_read",
                   "mc_counters_read", "mc_digests_read", "mc_nsample", "mc_histories_run",
-                  "mc_report", "mc_autotune", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
+                  "mc_report", "mc_autotune", "mc_lr_params", "mc_forward", "mc_backward", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
                   "mc_batch_autotune", "mc_batch_free"):
             getattr(L, f).restype = st
         _lib = L
@@ -216,6 +219,38 @@ class Problem:
 
     def report(self, path: str):
         self._check(lib().mc_report(self._h, os.fsencode(path)))
+
+    # ---- derivatives (one-group multigroup problems) ----
+    def lr_params(self) -> np.ndarray:
+        """The materials' one-group (Sigma_s, Sigma_a), interleaved."""
+        out = np.zeros(128)
+        self._check(lib().mc_lr_params(self._h, out.ctypes.data, 128))
+        return out[: 2 * self._n_materials()]
+
+    def _n_materials(self) -> int:
+        out = np.zeros(128)
+        lib().mc_lr_params(self._h, out.ctypes.data, 128)
+        nz = np.nonzero(out)[0]
+        return (int(nz[-1]) // 2 + 1) if nz.size else 0
+
+    def forward(self, params, n: int, seed: int = DEFAULT_SEED):
+        """(mean, sigma) of every tally bin at the given parameters."""
+        p = np.ascontiguousarray(params, np.float64)
+        nb = int(sum(self.sizes))
+        m = np.zeros(max(nb, 1))
+        s = np.zeros(max(nb, 1))
+        self._check(lib().mc_forward(self._h, p.ctypes.data, n, seed, m.ctypes.data, s.ctypes.data))
+        return m[:nb], s[:nb]
+
+    def backward(self, params, n: int, seed: int = DEFAULT_SEED):
+        """(d tally / d params, sigma), shaped [bins, params]."""
+        p = np.ascontiguousarray(params, np.float64)
+        nb = int(sum(self.sizes))
+        K = p.size
+        d = np.zeros(max(nb * K, 1))
+        s = np.zeros(max(nb * K, 1))
+        self._check(lib().mc_backward(self._h, p.ctypes.data, n, seed, d.ctypes.data, s.ctypes.data))
+        return d[: nb * K].reshape(nb, K), s[: nb * K].reshape(nb, K)
 
     def autotune(self, sample: int = 200000, seed: int = DEFAULT_SEED) -> dict:
         """Pick and keep the event engine's fastest launch shape."""
