@@ -125,6 +125,12 @@ struct Rng32 {
         draw = d;
         cached = 0;
     }
+    // hand in block 0 computed earlier in the same event
+    __device__ __forceinline__ void preload(uint32_t a, uint32_t b, uint32_t c, uint32_t d)
+    {
+        blk = U4{a, b, c, d};
+        cached = 1;
+    }
     __device__ __forceinline__ float next()
     {
         const uint32_t b = draw >> 2;
@@ -142,7 +148,8 @@ struct Rng32 {
 // shared-memory tile (SoA) and per-CTA bookkeeping
 struct Tile {
     float *x, *y, *z, *u, *v, *w, *E, *wt, *t, *sig, *frac;
-    int *cell, *surf, *hs, *g, *gi, *sense, *prob;
+    int *cell, *surf, *hs, *g, *gi, *sense, *prob, *xi;
+    uint32_t *b0, *b1, *b2, *b3;     // Philox block 0 of the current event
     uint32_t *id, *ev;
     unsigned short *qc, *qx;
     unsigned long long *hidx;
@@ -460,10 +467,48 @@ __device__ float score_value(Ctx &C, int sc, const PState &p, float l)
     }
 }
 
+// Estimator::score (Estimator.cpp:298-336) for estimators without a time
+// filter: every filter yields one (bin, length) pair or none, all lengths
+// equal l_in, so the combination loop collapses to one flattened index and
+// needs no pair list (which would live in local memory).
+__device__ __forceinline__ bool estimator_score_simple(Ctx &C, int e, const PState &p, float l_in)
+{
+    const EvTables &V = *C.V;
+    const int f0 = V.est_filt_off[e], nf = V.est_filt_off[e + 1] - f0;
+    const int *fac = V.est_factor + V.est_factor_off[e];
+    int idx1 = 0;
+    for (int i = 0; i < nf; ++i) {
+        const int f = f0 + i;
+        const float *grid = V.filt_grid + V.filt_grid_off[f];
+        const int glen = V.filt_grid_len[f];
+        int b;
+        switch (V.filt_kind[f]) {
+        case 0: b = bsearch_f((float)p.surf, grid, glen) + 1; if (b < 0 || b >= V.filt_size[f]) return true; break;
+        case 1: b = bsearch_f((float)p.cell, grid, glen) + 1; if (b < 0 || b >= V.filt_size[f]) return true; break;
+        case 2: b = bsearch_f(p.E, grid, glen); if (b < 0 || b >= glen - 1) return true; break;
+        case 4: b = p.g; break;
+        default: return false;          // time filter: take the general path
+        }
+        idx1 += b * fac[i + 1];
+    }
+    const int s0 = V.est_score_off[e], ns = V.est_score_off[e + 1] - s0;
+    const int base = V.est_bin_off[e];
+    for (int s = 0; s < ns; ++s) {
+        tally_add(C, p.hslot, base + idx1, (double)score_value(C, s0 + s, p, l_in));
+        idx1 += fac[0];
+    }
+    return true;
+}
+
 // Estimator::score (Estimator.cpp:298-336)
 __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, float speed, float l_in)
 {
     const EvTables &V = *C.V;
+    if (!(fabsf(l_in) <= FLT_MAX)) {   // non-finite track: the loop below would never advance
+        atomicCAS(C.s_status, 0, DS_NAN);
+        return;
+    }
+    if (estimator_score_simple(C, e, p, l_in)) return;
     const int f0 = V.est_filt_off[e], nf = V.est_filt_off[e + 1] - f0;
     const int s0 = V.est_score_off[e], ns = V.est_score_off[e + 1] - s0;
     const int *fac = V.est_factor + V.est_factor_off[e];
@@ -593,15 +638,13 @@ __device__ bool free_gas(Ctx &C, Rng32 &R, PState &p, float A)
     for (int it = 0;; ++it) {
         C.cnt[C_FREEGAS]++;
         if (it > (1 << 16)) return false;
-        float x;
-        if (R.next() < p_g2) {
-            const float a = R.next(), b = R.next();
-            x = sqrtf(-__logf(a * b));
-        } else {
-            const float cv = __cosf(kPiHalfF * R.next());
-            const float u1 = R.next(), u2 = R.next();
-            x = sqrtf(-__logf(u1) - __logf(u2) * cv * cv);
-        }
+        // Reaction.cpp:48-57 without the branch: the "w2" form
+        // sqrt(-ln(a b)) is the "w1" form sqrt(-ln u1 - ln u2 cos^2) with
+        // cos = 1, so a select keeps every lane of the warp on one path
+        const bool w2 = R.next() < p_g2;
+        const float u1 = R.next(), u2 = R.next(), u3 = R.next();
+        const float cv = w2 ? 1.f : __cosf(kPiHalfF * u3);
+        const float x = sqrtf(-__logf(u1) - __logf(u2) * (cv * cv));
         V = x / beta;
         mu = 2.f * R.next() - 1.f;
         const float acc = sqrtf(fmaxf(speed * speed + V * V - 2.f * speed * V * mu, 0.f)) / (speed + V);
@@ -724,6 +767,11 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
         takef(T.x); takef(T.y); takef(T.z); takef(T.u); takef(T.v); takef(T.w);
         takef(T.E); takef(T.wt); takef(T.t); takef(T.sig); takef(T.frac);
         takei(T.cell); takei(T.surf); takei(T.hs); takei(T.g); takei(T.gi); takei(T.sense); takei(T.prob);
+        takei(T.xi);
+        T.b0 = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
+        T.b1 = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
+        T.b2 = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
+        T.b3 = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
         T.id = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
         T.ev = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
         takei(T.live); takei(T.hfree); takei(T.hprob);
@@ -845,8 +893,17 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                 const int m = V.cell_mat[p.cell];
                 float sig = 0.f, dcol;
                 if (m >= 0) {
-                    sig = macro(C, m, XT, p);
+                    if (V.G > 0) {
+                        sig = macro(C, m, XT, p);
+                    } else {
+                        const XsAt a = xs_locate(V, m, p.E);
+                        sig = xs_at(V.gT, a);
+                        C.cnt[C_XS]++;
+                        T.xi[s] = a.i;
+                        T.frac[s] = a.f;
+                    }
                     dcol = -__logf(R.next()) / sig;
+                    T.b0[s] = R.blk.x; T.b1[s] = R.blk.y; T.b2[s] = R.blk.z; T.b3[s] = R.blk.w;
                 } else {
                     dcol = 0.9f * FLT_MAX;
                 }
@@ -901,6 +958,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
             C.cnt[C_COLL]++;
             bool alive = true;
             const int m = V.cell_mat[p.cell];
+            if (m >= 0) R.preload(T.b0[s], T.b1[s], T.b2[s], T.b3[s]);
             if (m < 0) {
                 alive = false;
             } else {
@@ -924,7 +982,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                     }
                     C.cnt[C_XS]++;
                 } else {
-                    const XsAt a = xs_locate(V, m, p.E);
+                    const XsAt a{m, T.xi[s], T.frac[s]};
                     const float sc = xs_at(V.gC, a);
                     const float ss = xs_at(V.gS, a);
                     C.cnt[C_XS] += 2;
@@ -1042,7 +1100,8 @@ size_t tile_smem_bytes(int P, long long nb_smem)
     b += sizeof(double) * 2 * (size_t)nb_smem;
     b += sizeof(unsigned long long) * P;
     b += 11 * sizeof(float) * P;
-    b += 7 * sizeof(int) * P;
+    b += 8 * sizeof(int) * P;
+    b += 4 * sizeof(uint32_t) * P;
     b += 2 * sizeof(uint32_t) * P;
     b += 3 * sizeof(int) * P;
     b += 2 * sizeof(unsigned short) * P;

@@ -1,0 +1,51 @@
+"""1-group slab (20 cm, Sigma_t = 1, c = 0.5, inward plane source with mu ~
+U(0,1]) against the deterministic S_N solution: transmission, reflection,
+absorption and the 100-bin track-length flux, in the production and the FP64
+modes."""
+import tempfile
+
+import numpy as np
+import pytest
+
+from stats import assert_agree
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mc():
+    import build as B
+    B.build()
+    import mcgpu
+    return mcgpu
+
+
+@pytest.fixture(scope="module")
+def reference():
+    from analytic import slab_1g_reference
+    return slab_1g_reference(dx_max=0.01, n_mu=64)
+
+
+@pytest.mark.parametrize("mode,n", [("event", 2_000_000), ("plain", 400_000), ("replay", 200_000)])
+def test_slab_against_sn(mc, reference, mode, n):
+    import mcgpu.workloads as W
+    with tempfile.TemporaryDirectory() as d:
+        W.slab_1g(d, samples=n)
+        p = mc.Problem(d, d + "/xs_library")
+        p.run(n=n, mode=mode)
+        T = p.tally(p.names.index("transmission"))
+        Rf = p.tally(p.names.index("reflection"))
+        S = p.tally(p.names.index("slab"))
+        p.close()
+    ref = reference
+    # reflection and absorption reach ~0.1 % relative error
+    assert abs(Rf[0][0] - ref["reflection"]) <= 3.5 * Rf[1][0] + 2e-4 * ref["reflection"]
+    absorption = float(np.sum(S[0][100:]))
+    abs_sigma = float(np.sqrt(np.sum(S[1][100:] ** 2)))   # bins are correlated: conservative
+    assert abs(absorption - ref["absorption"]) <= 3.5 * abs_sigma + 2e-4 * ref["absorption"]
+    # transmission through 20 mfp (~1.8e-9) is below what these histories resolve
+    assert T[0][0] <= ref["transmission"] + 4 * max(T[1][0], 1.0 / n)
+    # the flux profile, bin by bin (S_N mesh error ~1e-4 relative)
+    flux, fsig = S[0][:100], S[1][:100]
+    tol = np.sqrt(fsig ** 2 + (2e-4 * ref["flux"]) ** 2)
+    assert_agree(flux, tol, ref["flux"], np.zeros(100), f"{mode} flux profile")
