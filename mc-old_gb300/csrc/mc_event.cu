@@ -145,16 +145,68 @@ struct Rng32 {
     }
 };
 
-// shared-memory tile (SoA) and per-CTA bookkeeping
+// shared-memory tile (SoA) and per-CTA bookkeeping.  Every array is addressed
+// from the dynamic shared-memory base and the tile size P, so the tile costs
+// two registers instead of one pointer per array.  Layout (bytes):
+//   [hidx: 8P][28 four-byte arrays: 4P each][qc: 2P][qx: 2P][ssum, ssq: 8 nb each]
+enum TileArray {
+    TA_X, TA_Y, TA_Z, TA_U, TA_V, TA_W, TA_E, TA_WT, TA_T, TA_SIG, TA_FRAC,
+    TA_CELL, TA_SURF, TA_HS, TA_G, TA_GI, TA_SENSE, TA_PROB, TA_XI,
+    TA_B0, TA_B1, TA_B2, TA_B3,          // Philox block 0 of the current event
+    TA_ID, TA_EV, TA_LIVE, TA_HFREE, TA_HPROB,
+    TA_COUNT
+};
+
 struct Tile {
-    float *x, *y, *z, *u, *v, *w, *E, *wt, *t, *sig, *frac;
-    int *cell, *surf, *hs, *g, *gi, *sense, *prob, *xi;
-    uint32_t *b0, *b1, *b2, *b3;     // Philox block 0 of the current event
-    uint32_t *id, *ev;
-    unsigned short *qc, *qx;
-    unsigned long long *hidx;
-    int *live, *hfree, *hprob;
-    double *ssum, *ssq;
+    unsigned char *base;
+    int P;
+    long long nsum;                      // bins of the per-CTA sums (0: none)
+    template <typename X> __device__ __forceinline__ X *a4(int k) const
+    {
+        return reinterpret_cast<X *>(base + 8 * P + 4 * P * k);
+    }
+    __device__ __forceinline__ float *x() const { return a4<float>(TA_X); }
+    __device__ __forceinline__ float *y() const { return a4<float>(TA_Y); }
+    __device__ __forceinline__ float *z() const { return a4<float>(TA_Z); }
+    __device__ __forceinline__ float *u() const { return a4<float>(TA_U); }
+    __device__ __forceinline__ float *v() const { return a4<float>(TA_V); }
+    __device__ __forceinline__ float *w() const { return a4<float>(TA_W); }
+    __device__ __forceinline__ float *E() const { return a4<float>(TA_E); }
+    __device__ __forceinline__ float *wt() const { return a4<float>(TA_WT); }
+    __device__ __forceinline__ float *t() const { return a4<float>(TA_T); }
+    __device__ __forceinline__ float *sig() const { return a4<float>(TA_SIG); }
+    __device__ __forceinline__ float *frac() const { return a4<float>(TA_FRAC); }
+    __device__ __forceinline__ int *cell() const { return a4<int>(TA_CELL); }
+    __device__ __forceinline__ int *surf() const { return a4<int>(TA_SURF); }
+    __device__ __forceinline__ int *hs() const { return a4<int>(TA_HS); }
+    __device__ __forceinline__ int *g() const { return a4<int>(TA_G); }
+    __device__ __forceinline__ int *gi() const { return a4<int>(TA_GI); }
+    __device__ __forceinline__ int *sense() const { return a4<int>(TA_SENSE); }
+    __device__ __forceinline__ int *prob() const { return a4<int>(TA_PROB); }
+    __device__ __forceinline__ int *xi() const { return a4<int>(TA_XI); }
+    __device__ __forceinline__ uint32_t *b0() const { return a4<uint32_t>(TA_B0); }
+    __device__ __forceinline__ uint32_t *b1() const { return a4<uint32_t>(TA_B1); }
+    __device__ __forceinline__ uint32_t *b2() const { return a4<uint32_t>(TA_B2); }
+    __device__ __forceinline__ uint32_t *b3() const { return a4<uint32_t>(TA_B3); }
+    __device__ __forceinline__ uint32_t *id() const { return a4<uint32_t>(TA_ID); }
+    __device__ __forceinline__ uint32_t *ev() const { return a4<uint32_t>(TA_EV); }
+    __device__ __forceinline__ int *live() const { return a4<int>(TA_LIVE); }
+    __device__ __forceinline__ int *hfree() const { return a4<int>(TA_HFREE); }
+    __device__ __forceinline__ int *hprob() const { return a4<int>(TA_HPROB); }
+    __device__ __forceinline__ unsigned long long *hidx() const
+    {
+        return reinterpret_cast<unsigned long long *>(base);
+    }
+    __device__ __forceinline__ unsigned short *qc() const
+    {
+        return reinterpret_cast<unsigned short *>(base + 8 * P + 4 * P * TA_COUNT);
+    }
+    __device__ __forceinline__ unsigned short *qx() const { return qc() + P; }
+    __device__ __forceinline__ double *ssum() const
+    {
+        return reinterpret_cast<double *>(base + 8 * P + 4 * P * TA_COUNT + 4 * P);
+    }
+    __device__ __forceinline__ double *ssq() const { return ssum() + nsum; }
 };
 
 struct PState {
@@ -165,25 +217,25 @@ struct PState {
 
 __device__ __forceinline__ void load_p(const Tile &T, int s, PState &p)
 {
-    p.x = T.x[s]; p.y = T.y[s]; p.z = T.z[s]; p.u = T.u[s]; p.v = T.v[s]; p.w = T.w[s];
-    p.E = T.E[s]; p.wt = T.wt[s]; p.t = T.t[s];
-    p.cell = T.cell[s]; p.surf = T.surf[s]; p.hslot = T.hs[s]; p.g = T.g[s]; p.prob = T.prob[s];
-    p.id = T.id[s]; p.ev = T.ev[s];
+    p.x = T.x()[s]; p.y = T.y()[s]; p.z = T.z()[s]; p.u = T.u()[s]; p.v = T.v()[s]; p.w = T.w()[s];
+    p.E = T.E()[s]; p.wt = T.wt()[s]; p.t = T.t()[s];
+    p.cell = T.cell()[s]; p.surf = T.surf()[s]; p.hslot = T.hs()[s]; p.g = T.g()[s]; p.prob = T.prob()[s];
+    p.id = T.id()[s]; p.ev = T.ev()[s];
 }
 
 __device__ __forceinline__ void store_p(const Tile &T, int s, const PState &p)
 {
-    T.x[s] = p.x; T.y[s] = p.y; T.z[s] = p.z; T.u[s] = p.u; T.v[s] = p.v; T.w[s] = p.w;
-    T.E[s] = p.E; T.wt[s] = p.wt; T.t[s] = p.t;
-    T.cell[s] = p.cell; T.surf[s] = p.surf; T.hs[s] = p.hslot; T.g[s] = p.g; T.prob[s] = p.prob;
-    T.id[s] = p.id; T.ev[s] = p.ev;
+    T.x()[s] = p.x; T.y()[s] = p.y; T.z()[s] = p.z; T.u()[s] = p.u; T.v()[s] = p.v; T.w()[s] = p.w;
+    T.E()[s] = p.E; T.wt()[s] = p.wt; T.t()[s] = p.t;
+    T.cell()[s] = p.cell; T.surf()[s] = p.surf; T.hs()[s] = p.hslot; T.g()[s] = p.g; T.prob()[s] = p.prob;
+    T.id()[s] = p.id; T.ev()[s] = p.ev;
 }
 
 struct Ctx {
     const EvTables *V;            // tables of the particle being processed
     const EvArgs *A;
     Tile T;
-    unsigned long long cnt[kNumCounters];
+    uint32_t cnt[kNumCounters];   // per-thread event counters, spilled to A.counters near 2^30
     int *s_status;
     int *s_novf;
     int *s_nlive;
@@ -561,7 +613,7 @@ __device__ void history_fold(Ctx &C, int hslot)
     unsigned long long *mask = C.A->mask + row * C.A->nw;
     double *gs = C.A->sum, *gq = C.A->sq;
     if (C.A->n_prob > 0) {
-        const int pr = C.T.hprob[hslot];
+        const int pr = C.T.hprob()[hslot];
         gs = C.A->psum[pr];
         gq = C.A->psq[pr];
     }
@@ -575,8 +627,8 @@ __device__ void history_fold(Ctx &C, int hslot)
             const double v = __longlong_as_double(
                 (long long)atomicExch(reinterpret_cast<unsigned long long *>(acc + bin), 0ull));
             if (C.A->smem_sums) {
-                atomicAdd(C.T.ssum + bin, v);
-                atomicAdd(C.T.ssq + bin, v * v);
+                atomicAdd(C.T.ssum() + bin, v);
+                atomicAdd(C.T.ssq() + bin, v * v);
             } else {
                 atomicAdd(gs + bin, v);
                 atomicAdd(gq + bin, v * v);
@@ -587,13 +639,13 @@ __device__ void history_fold(Ctx &C, int hslot)
 
 __device__ __forceinline__ void particle_dies(Ctx &C, int s, int hslot)
 {
-    C.T.hs[s] = -1;
+    C.T.hs()[s] = -1;
     atomicSub(C.s_nlive, 1);
-    if (atomicSub(&C.T.live[hslot], 1) == 1) {
+    if (atomicSub(&C.T.live()[hslot], 1) == 1) {
         __threadfence_block();
         history_fold(C, hslot);
         const int k = atomicAdd(C.s_nhfree, 1);
-        C.T.hfree[k] = hslot;
+        C.T.hfree()[k] = hslot;
     }
 }
 
@@ -755,29 +807,9 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     const int P = A.tile;
     const int H = P;
     Tile T;
-    {
-        unsigned char *q = smem;
-        auto takef = [&](float *&ptr) { ptr = reinterpret_cast<float *>(q); q += sizeof(float) * P; };
-        auto takei = [&](int *&ptr) { ptr = reinterpret_cast<int *>(q); q += sizeof(int) * P; };
-        const long long nsum = A.smem_sums ? V0.n_bins : 0;
-        double *d = reinterpret_cast<double *>(q);
-        T.ssum = d; T.ssq = d + nsum;
-        q += sizeof(double) * 2 * nsum;
-        T.hidx = reinterpret_cast<unsigned long long *>(q); q += sizeof(unsigned long long) * H;
-        takef(T.x); takef(T.y); takef(T.z); takef(T.u); takef(T.v); takef(T.w);
-        takef(T.E); takef(T.wt); takef(T.t); takef(T.sig); takef(T.frac);
-        takei(T.cell); takei(T.surf); takei(T.hs); takei(T.g); takei(T.gi); takei(T.sense); takei(T.prob);
-        takei(T.xi);
-        T.b0 = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
-        T.b1 = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
-        T.b2 = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
-        T.b3 = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
-        T.id = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
-        T.ev = reinterpret_cast<uint32_t *>(q); q += sizeof(uint32_t) * P;
-        takei(T.live); takei(T.hfree); takei(T.hprob);
-        T.qc = reinterpret_cast<unsigned short *>(q); q += sizeof(unsigned short) * P;
-        T.qx = reinterpret_cast<unsigned short *>(q); q += sizeof(unsigned short) * P;
-    }
+    T.base = smem;
+    T.P = P;
+    T.nsum = A.smem_sums ? V0.n_bins : 0;
     __shared__ int s_nlive, s_novf, s_nhfree, s_status, s_nqc, s_nqx, s_rank;
     __shared__ int s_take_ovf, s_got, s_ovf_base, s_hfree_base, s_exhausted;
     __shared__ unsigned long long s_hist_base;
@@ -795,12 +827,12 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
 
     for (int s = threadIdx.x; s < P; s += blockDim.x) {
-        T.hs[s] = -1;
-        T.hfree[s] = s;
-        T.live[s] = 0;
+        T.hs()[s] = -1;
+        T.hfree()[s] = s;
+        T.live()[s] = 0;
     }
     if (A.smem_sums)
-        for (int b = threadIdx.x; b < 2 * V0.n_bins; b += blockDim.x) T.ssum[b] = 0.0;
+        for (int b = threadIdx.x; b < 2 * V0.n_bins; b += blockDim.x) T.ssum()[b] = 0.0;
     if (threadIdx.x == 0) {
         s_nlive = 0; s_novf = 0; s_nhfree = H; s_status = 0; s_nqc = 0; s_nqx = 0;
         s_exhausted = 0;
@@ -810,7 +842,12 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
 
     for (;;) {
         // ---------------- refill ----------------
+        // one thread books the refill; every read of the previous event's
+        // queue counters happened before the barrier that closed it
         if (threadIdx.x == 0) {
+            s_nqc = 0;
+            s_nqx = 0;
+            if (s_novf > A.ovf_cap) s_novf = A.ovf_cap;
             const int free_slots = P - s_nlive;
             const int take = min(free_slots, s_novf);
             s_take_ovf = take;
@@ -835,48 +872,57 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
             s_rank = 0;
         }
         __syncthreads();
+        {
+            // one event adds at most 2^16 + a few to a counter: hand the
+            // 32-bit counters to the global 64-bit ones well before they wrap
+            uint32_t big = 0;
+            for (int i = 0; i < kNumCounters; ++i) big |= C.cnt[i];
+            if (big >= (1u << 30))
+                for (int i = 0; i < kNumCounters; ++i) {
+                    atomicAdd(A.counters + i, (unsigned long long)C.cnt[i]);
+                    C.cnt[i] = 0;
+                }
+        }
         if (s_nlive == 0 && s_novf == 0 && (s_exhausted || s_status != 0)) break;
         if (s_status != 0) break;
+        // ---------------- refill + advance ----------------
+        // the thread that refills slot s also advances it, so no barrier
+        // separates the two
         for (int s0 = 0; s0 < P; s0 += blockDim.x) {
             const int s = s0 + threadIdx.x;
-            const bool is_free = s < P && T.hs[s] < 0;
+            const bool is_free = s < P && T.hs()[s] < 0;
             const int r = warp_append(&s_rank, is_free);
-            if (!is_free) continue;
-            PState p;
-            if (r < s_take_ovf) {
-                const OvfP &o = ovf[s_ovf_base + r];
-                p.x = o.x; p.y = o.y; p.z = o.z; p.u = o.u; p.v = o.v; p.w = o.w;
-                p.E = o.E; p.wt = o.wt; p.t = o.t; p.cell = o.cell; p.surf = o.surf;
-                p.hslot = o.hslot; p.g = o.g; p.id = o.id; p.ev = 0u;
-                p.prob = T.hprob[o.hslot];
-                store_p(T, s, p);
-                C.cnt[C_PART]++;
-            } else if (r - s_take_ovf < s_got) {
-                const int k = r - s_take_ovf;
-                const int hslot = T.hfree[s_hfree_base + k];
-                const unsigned long long gi = s_hist_base + (unsigned long long)k;
-                int prob = 0;
-                uint64_t hist = A.first + gi;
-                if (kBatch) {
-                    prob = problem_of(A, gi);
-                    hist = gi - A.prefix[prob];
+            if (is_free) {
+                PState p;
+                if (r < s_take_ovf) {
+                    const OvfP &o = ovf[s_ovf_base + r];
+                    p.x = o.x; p.y = o.y; p.z = o.z; p.u = o.u; p.v = o.v; p.w = o.w;
+                    p.E = o.E; p.wt = o.wt; p.t = o.t; p.cell = o.cell; p.surf = o.surf;
+                    p.hslot = o.hslot; p.g = o.g; p.id = o.id; p.ev = 0u;
+                    p.prob = T.hprob()[o.hslot];
+                    store_p(T, s, p);
+                    C.cnt[C_PART]++;
+                } else if (r - s_take_ovf < s_got) {
+                    const int k = r - s_take_ovf;
+                    const int hslot = T.hfree()[s_hfree_base + k];
+                    const unsigned long long gi = s_hist_base + (unsigned long long)k;
+                    int prob = 0;
+                    uint64_t hist = A.first + gi;
+                    if (kBatch) {
+                        prob = problem_of(A, gi);
+                        hist = gi - A.prefix[prob];
+                    }
+                    T.hidx()[hslot] = hist;
+                    T.hprob()[hslot] = prob;
+                    T.live()[hslot] = 1;
+                    sample_source(tab(prob), seed_of(prob), hist, p);
+                    p.hslot = hslot;
+                    p.prob = prob;
+                    store_p(T, s, p);
+                    C.cnt[C_PART]++;
                 }
-                T.hidx[hslot] = hist;
-                T.hprob[hslot] = prob;
-                T.live[hslot] = 1;
-                sample_source(tab(prob), seed_of(prob), hist, p);
-                p.hslot = hslot;
-                p.prob = prob;
-                store_p(T, s, p);
-                C.cnt[C_PART]++;
             }
-        }
-        __syncthreads();
-
-        // ---------------- advance ----------------
-        for (int s0 = 0; s0 < P; s0 += blockDim.x) {
-            const int s = s0 + threadIdx.x;
-            const bool live = s < P && T.hs[s] >= 0;
+            const bool live = s < P && T.hs()[s] >= 0;
             int kind = 0;   // 1 collide, 2 cross
             if (live) {
                 PState p;
@@ -889,7 +935,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                     p.ev = kMaxEvents;
                 }
                 Rng32 R;
-                R.init(seed_of(p.prob), T.hidx[p.hslot], p.id, p.ev, 0u);
+                R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 0u);
                 const int m = V.cell_mat[p.cell];
                 float sig = 0.f, dcol;
                 if (m >= 0) {
@@ -899,11 +945,11 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                         const XsAt a = xs_locate(V, m, p.E);
                         sig = xs_at(V.gT, a);
                         C.cnt[C_XS]++;
-                        T.xi[s] = a.i;
-                        T.frac[s] = a.f;
+                        T.xi()[s] = a.i;
+                        T.frac()[s] = a.f;
                     }
                     dcol = -__logf(R.next()) / sig;
-                    T.b0[s] = R.blk.x; T.b1[s] = R.blk.y; T.b2[s] = R.blk.z; T.b3[s] = R.blk.w;
+                    T.b0()[s] = R.blk.x; T.b1()[s] = R.blk.y; T.b2()[s] = R.blk.z; T.b3()[s] = R.blk.w;
                 } else {
                     dcol = 0.9f * FLT_MAX;
                 }
@@ -925,46 +971,46 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                         p.t = t_old + l / speed;
                     }
                     C.cnt[C_FLIGHTS]++;
-                    if (m >= 0 && V.G == 0) C.cnt[C_NUC] += (unsigned long long)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
+                    if (m >= 0 && V.G == 0) C.cnt[C_NUC] += (uint32_t)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
                     for (int i = V.cell_tl_off[p.cell]; i < V.cell_tl_off[p.cell + 1]; ++i)
                         estimator_score(C, V.cell_tl[i], p, t_old, speed, l);
                     p.surf = -1;
                     kind = cross ? 2 : 1;
-                    T.gi[s] = S;
-                    T.sense[s] = sense;
-                    T.sig[s] = sig;
+                    T.gi()[s] = S;
+                    T.sense()[s] = sense;
+                    T.sig()[s] = sig;
                 } else {
                     atomicCAS(&s_status, 0, DS_LOST);
                 }
                 store_p(T, s, p);
             }
             const int pc = warp_append(&s_nqc, kind == 1);
-            if (kind == 1) T.qc[pc] = (unsigned short)s;
+            if (kind == 1) T.qc()[pc] = (unsigned short)s;
             const int px = warp_append(&s_nqx, kind == 2);
-            if (kind == 2) T.qx[px] = (unsigned short)s;
+            if (kind == 2) T.qx()[px] = (unsigned short)s;
         }
         __syncthreads();
 
         // ---------------- collide ----------------
         const int nqc = s_nqc;
         for (int j = threadIdx.x; j < nqc; j += blockDim.x) {
-            const int s = T.qc[j];
+            const int s = T.qc()[j];
             PState p;
             load_p(T, s, p);
             const EvTables &V = tab(p.prob);
             C.V = &V;
             Rng32 R;
-            R.init(seed_of(p.prob), T.hidx[p.hslot], p.id, p.ev, 1u);
+            R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 1u);
             C.cnt[C_COLL]++;
             bool alive = true;
             const int m = V.cell_mat[p.cell];
-            if (m >= 0) R.preload(T.b0[s], T.b1[s], T.b2[s], T.b3[s]);
+            if (m >= 0) R.preload(T.b0()[s], T.b1()[s], T.b2()[s], T.b3()[s]);
             if (m < 0) {
                 alive = false;
             } else {
                 for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
                     estimator_score(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f);
-                const float st = T.sig[s];
+                const float st = T.sig()[s];
                 if (V.G > 0) {
                     const int row = m * V.G + p.g;
                     p.wt = p.wt * (st - __ldg(V.mg_capture + row)) / st;
@@ -982,7 +1028,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                     }
                     C.cnt[C_XS]++;
                 } else {
-                    const XsAt a{m, T.xi[s], T.frac[s]};
+                    const XsAt a{m, T.xi()[s], T.frac()[s]};
                     const float sc = xs_at(V.gC, a);
                     const float ss = xs_at(V.gS, a);
                     C.cnt[C_XS] += 2;
@@ -1009,21 +1055,21 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
         // ---------------- cross ----------------
         const int nqx = s_nqx;
         for (int j = threadIdx.x; j < nqx; j += blockDim.x) {
-            const int s = T.qx[j];
+            const int s = T.qx()[j];
             PState p;
             load_p(T, s, p);
             const EvTables &V = tab(p.prob);
             C.V = &V;
             Rng32 R;
-            R.init(seed_of(p.prob), T.hidx[p.hslot], p.id, p.ev, 1u);
+            R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 1u);
             C.cnt[C_CROSS]++;
-            const int S = T.gi[s];
+            const int S = T.gi()[s];
             const int old_cell = p.cell;
             bool alive = true;
             const int bc = V.surf_bc[S];
             p.surf = S;
             if (bc == 0) {
-                const bool pos = !(T.sense[s] > 0);
+                const bool pos = !(T.sense()[s] > 0);
                 const int c = cell_across(V, p, S, pos);
                 if (c < 0) { atomicCAS(&s_status, 0, DS_LOST); alive = false; }
                 else p.cell = c;
@@ -1058,7 +1104,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                             o.hslot = p.hslot; o.g = p.g;
                             o.id = child_id(p.id, p.ev, (uint32_t)k);
                             ovf[slot] = o;
-                            atomicAdd(&T.live[p.hslot], 1);
+                            atomicAdd(&T.live()[p.hslot], 1);
                             C.cnt[C_SPLIT]++;
                         }
                     }
@@ -1069,26 +1115,20 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
             else particle_dies(C, s, p.hslot);
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            s_nqc = 0;
-            s_nqx = 0;
-            if (s_novf > A.ovf_cap) s_novf = A.ovf_cap;
-        }
-        __syncthreads();
     }
 
     // flush per-CTA sums and counters
     __syncthreads();
     if (A.smem_sums) {
         for (int b = threadIdx.x; b < V0.n_bins; b += blockDim.x) {
-            const double sv = T.ssum[b], qv = T.ssq[b];
+            const double sv = T.ssum()[b], qv = T.ssq()[b];
             if (sv != 0.0) atomicAdd(A.sum + b, sv);
             if (qv != 0.0) atomicAdd(A.sq + b, qv);
         }
     }
     if (threadIdx.x == 0 && s_status != 0) atomicCAS(A.status, 0, s_status);
     for (int i = 0; i < kNumCounters; ++i) {
-        unsigned long long v = C.cnt[i];
+        unsigned long long v = C.cnt[i];   // a warp's sum needs 64 bits
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if ((threadIdx.x & 31) == 0 && v) atomicAdd(A.counters + i, v);
     }
@@ -1096,16 +1136,8 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
 
 size_t tile_smem_bytes(int P, long long nb_smem)
 {
-    size_t b = 0;
-    b += sizeof(double) * 2 * (size_t)nb_smem;
-    b += sizeof(unsigned long long) * P;
-    b += 11 * sizeof(float) * P;
-    b += 8 * sizeof(int) * P;
-    b += 4 * sizeof(uint32_t) * P;
-    b += 2 * sizeof(uint32_t) * P;
-    b += 3 * sizeof(int) * P;
-    b += 2 * sizeof(unsigned short) * P;
-    return b + 64;
+    // the layout of Tile: hidx, the four-byte arrays, qc / qx, the sums
+    return (size_t)P * (8 + 4 * TA_COUNT + 2 * sizeof(unsigned short)) + sizeof(double) * 2 * (size_t)nb_smem + 64;
 }
 
 typedef void (*EvKernel)(const EvTables, const EvArgs);

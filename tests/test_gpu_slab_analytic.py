@@ -45,7 +45,11 @@ def test_slab_against_sn(mc, reference, mode, n):
     assert abs(absorption - ref["absorption"]) <= 3.5 * abs_sigma + 2e-4 * ref["absorption"]
     # transmission through 20 mfp (~1.8e-9) is below what these histories resolve
     assert T[0][0] <= ref["transmission"] + 4 * max(T[1][0], 1.0 / n)
-    # the flux profile, bin by bin (S_N mesh error ~1e-4 relative)
+    # the flux profile, bin by bin (S_N mesh error ~1e-4 relative), over the
+    # bins these histories resolve to 5 % or better: deeper bins hold a few
+    # scores or none, and a bin without scores has no error estimate
     flux, fsig = S[0][:100], S[1][:100]
-    tol = np.sqrt(fsig ** 2 + (2e-4 * ref["flux"]) ** 2)
-    assert_agree(flux, tol, ref["flux"], np.zeros(100), f"{mode} flux profile")
+    ok = (fsig > 0) & (fsig <= 0.05 * flux)
+    assert ok[:20].all() and ok.sum() >= 20, ok
+    tol = np.sqrt(fsig[ok] ** 2 + (2e-4 * ref["flux"][ok]) ** 2)
+    assert_agree(flux[ok], tol, ref["flux"][ok], np.zeros(int(ok.sum())), f"{mode} flux profile")
