@@ -13,6 +13,7 @@ struct DevTables {
     int n_surf, n_cell, n_mat, n_nuc, mg_groups, n_est, n_src;
     long long n_bins;
     double wr, ws;
+    int comb_bank_max, comb_teeth;     // particle comb (0 teeth: off)
     const int *surf_type, *surf_bc;
     const double *surf_coef;
     const double *cell_imp;

@@ -89,6 +89,7 @@ mc_status device_problem_init(const Tables &t, DeviceProblem &d, std::string &er
     T.mg_groups = t.mg_groups; T.n_est = t.n_est(); T.n_src = t.n_src();
     T.n_bins = t.n_bins();
     T.wr = t.wr; T.ws = t.ws;
+    T.comb_bank_max = t.comb_bank_max; T.comb_teeth = t.comb_teeth;
     Packer P;
     P.add(t.surf_type, &T.surf_type); P.add(t.surf_bc, &T.surf_bc); P.add(t.surf_coef, &T.surf_coef);
     P.add(t.cell_imp, &T.cell_imp); P.add(t.cell_mat, &T.cell_mat); P.add(t.cell_surf_off, &T.cell_surf_off);
@@ -210,7 +211,9 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
 {
     const int block = (tune && tune->block) ? (int)tune->block : 128;
     if (block != 128) { err = "FP64 history kernels are built for 128-thread blocks"; return MC_ERR_ARG; }
-    const uint32_t depth = (tune && tune->stack_depth) ? tune->stack_depth : 32;
+    uint32_t depth = (tune && tune->stack_depth) ? tune->stack_depth : 32;
+    // a combed bank holds `teeth` particles plus the split copies of one walk
+    if (t.comb_teeth > 0 && !(tune && tune->stack_depth)) depth = std::max<uint32_t>(depth, (uint32_t)t.comb_teeth + 32);
     const bool want_digest = tune && tune->record_digests;
     int max_threads = history_fp64_max_threads(replay, block);
     int grid = (tune && tune->grid_blocks) ? (int)tune->grid_blocks : max_threads / block;

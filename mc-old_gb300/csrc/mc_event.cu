@@ -1162,6 +1162,12 @@ EvKernel pick_kernel(int minb, bool batch)
 
 bool event_tables_ready(const Tables &t, DeviceProblem &d, std::string &err)
 {
+    if (t.comb_teeth > 0) {
+        // the comb acts on one history's bank after each walk; the event
+        // engine runs a history's particles side by side and has no such bank
+        err = "the particle comb needs the history-ordered FP64 modes (MC_FP64_REPLAY or MC_FP64_PLAIN)";
+        return false;
+    }
     if (d.ev_state) return true;
     EventState *S = new EventState();
     if (!build_event_tables(t, S->host, err)) { delete S; return false; }

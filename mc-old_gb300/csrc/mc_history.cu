@@ -676,6 +676,44 @@ __device__ void random_walk(Ctx &C, PartD &p, bool digests)
     }
 }
 
+// population_control.cpp:55-84, after every random walk (handler.cpp:27), on
+// the thread's bank.  The first tooth is the one draw, from the stream of the
+// particle that just walked at event kCombEvent.  A particle passes at most
+// one tooth (the reference's `if`), and tooth j is filled from a bank entry
+// i >= j, so the bank is compacted in place; the teeth left over hold the
+// bank's first particle with its own weight (bank_tmp(teeth, Pbank[0])).
+// The copies get ids child_id(walker, kCombEvent, j + 1).
+constexpr uint32_t kCombEvent = 0xFFFFFFFFu;
+
+__device__ void particle_comb(Ctx &C, uint32_t walker)
+{
+    const DevTables &T = *C.T;
+    if (C.sp < T.comb_bank_max) return;
+    const int teeth = T.comb_teeth;
+    if (teeth > C.depth) { C.status = DS_OVERFLOW; return; }
+    double W = 0.0;
+    for (int i = 0; i < C.sp; ++i) W += C.stack[i].wgt;
+    const double w_avg = W / (double)teeth;
+    C.rng.id = walker;
+    C.rng.start_event(kCombEvent);
+    double tooth = C.rng.next() * w_avg;
+    const PartD first = C.stack[0];
+    double sum = 0.0;
+    int j = 0;
+    for (int i = 0; i < C.sp; ++i) {
+        sum += C.stack[i].wgt;
+        if (sum > tooth && j < teeth) {   // j < teeth: rounding cannot add a tooth
+            PartD q = C.stack[i];
+            q.wgt = w_avg;
+            C.stack[j++] = q;
+            tooth += w_avg;
+        }
+    }
+    for (int k = j; k < teeth; ++k) C.stack[k] = first;
+    C.sp = teeth;
+    for (int k = 0; k < teeth; ++k) C.stack[k].id = child_id(walker, kCombEvent, (uint32_t)(k + 1));
+}
+
 // Source.cpp:20-24, 42-45 and Distribution.cpp:30-33, 78-96
 template <bool R>
 __device__ void sample_source(Ctx &C, PartD &p)
@@ -749,12 +787,17 @@ __global__ void __launch_bounds__(128) k_history_fp64(const DevTables T, const H
         if constexpr (L)
             for (int k = 0; k < C.K; ++k) C.lr_stack[k] = 0.0;
         C.stack[C.sp++] = p;
+        uint32_t walks = 0;
         while (C.sp > 0 && C.status == DS_OK) {
             --C.sp;
             PartD q = C.stack[C.sp];
             if constexpr (L)
                 for (int k = 0; k < C.K; ++k) C.S[k] = C.lr_stack[(size_t)C.sp * C.K + k];
+            if (++walks > (1u << 24)) { C.status = DS_TIMEOUT; break; }   // bounded history
             random_walk<R, L>(C, q, digests);
+            // the derivative kernels refuse combed problems on the host
+            if constexpr (!L)
+                if (T.comb_teeth > 0 && C.status == DS_OK) particle_comb(C, q.id);
         }
         if (digests) A.digest[hl] = C.digest;
         if (C.status != DS_OK) {

@@ -46,6 +46,7 @@ mc_status check_one_group(mc_problem *p, const double *params)
         p->err = "forward/backward need a one-group multigroup problem (<multigroup groups=\"1\"/>)";
         return MC_ERR_ARG;
     }
+    if (p->t.comb_teeth > 0) { p->err = "forward/backward do not support the particle comb"; return MC_ERR_ARG; }
     if (2 * p->t.n_mat() > kMaxLrParams) { p->err = "forward/backward support at most 32 materials"; return MC_ERR_ARG; }
     for (int i = 0; i < 2 * p->t.n_mat(); ++i)
         if (!(params[i] >= 0.0) || !std::isfinite(params[i])) { p->err = "cross sections must be finite and >= 0"; return MC_ERR_ARG; }

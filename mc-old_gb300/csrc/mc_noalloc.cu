@@ -69,6 +69,11 @@ extern "C" mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first, uint64
     if (!p || !d_sum || !d_sumsq) return MC_ERR_ARG;
     if (!p->dev.ready) { p->err = "problem was not loaded"; return MC_ERR_ARG; }
     DeviceProblem &d = p->dev;
+    if (d.dt.comb_teeth > (int)kDepth / 2) {
+        p->err = "mc_run_replay_noalloc: a particle comb with more than " + std::to_string(kDepth / 2) +
+                 " teeth does not fit the fixed split stack";
+        return MC_ERR_ARG;
+    }
     const long long nb = std::max<long long>(d.dt.n_bins, 1);
     const size_t stack_bytes = (size_t)kThreads * kDepth * fp64_particle_bytes();
     const size_t row_bytes = (size_t)nb * sizeof(double);

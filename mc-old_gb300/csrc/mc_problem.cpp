@@ -118,7 +118,20 @@ bool load_problem(const std::string &io_dir, const std::string &xs_dir, Tables &
 
     // ---- population control (setup.cpp:57-67, simulator.h:90-91) ----
     if (const XmlNode *ctrl = doc.child("population_control")) {
-        if (ctrl->child("particle_comb")) { err = "particle comb is not supported on this path"; return false; }
+        if (const XmlNode *c = ctrl->child("particle_comb")) {
+            t.comb_bank_max = (int32_t)c->as_int("bank_max");
+            t.comb_teeth = (int32_t)c->as_int("teeth");
+            if (t.comb_bank_max < 1 || t.comb_teeth < 1) {
+                err = "<particle_comb> needs bank_max >= 1 and teeth >= 1";
+                return false;
+            }
+            // with more teeth than bank_max, the combed bank is still at least
+            // bank_max after the next pop and the history never ends
+            if (t.comb_teeth > t.comb_bank_max) {
+                err = "<particle_comb> teeth > bank_max never empties the bank";
+                return false;
+            }
+        }
         if (const XmlNode *w = ctrl->child("weight_roulette")) {
             t.wr = w->as_double("wr", t.wr);
             t.ws = w->as_double("ws", t.ws);

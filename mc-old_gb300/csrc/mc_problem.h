@@ -39,6 +39,7 @@ struct Tables {
     std::string name;
     uint64_t nsample = 0;
     double wr = 0.001, ws = 1.0;
+    int32_t comb_bank_max = 0, comb_teeth = 0;   // particle comb (0 teeth: off)
 
     std::vector<int32_t> surf_type, surf_bc;
     std::vector<double> surf_coef;

@@ -801,6 +801,53 @@ static void sample_source(orc_ctx *C, orc_particle *p)
     p->id = 0;
 }
 
+/* Simulator::particle_comb (population_control.cpp:55-84), called after every
+ * random walk (handler.cpp:27) on the history's bank.  The one draw (the first
+ * tooth) comes from the stream of the particle that just walked, at event
+ * ORC_COMB_EVENT.  Every particle passes at most one tooth (the reference's
+ * `if`, not a loop), so the comb keeps at most one copy of each particle; the
+ * teeth left over keep the bank's first particle with its own weight, as the
+ * reference's bank_tmp(comb_teeth, Pbank[0]) does.  Because tooth j is filled
+ * from a particle i >= j, the comb compacts the bank in place.  The copies get
+ * fresh ids orc_child_id(walker, ORC_COMB_EVENT, j + 1) so that the teeth do
+ * not share random streams. */
+#define ORC_COMB_EVENT 0xFFFFFFFFu
+static void particle_comb(orc_ctx *C, uint32_t walker)
+{
+    const orc_problem *P = C->P;
+    orc_stack *b = &C->bank;
+    if (b->n < (size_t)P->comb_bank_max) return;
+    double W = 0.0;
+    for (size_t i = 0; i < b->n; ++i) W += b->v[i].wgt;
+    const double w_avg = W / (double)P->comb_teeth;
+    C->rng.id = walker;
+    C->rng.event = ORC_COMB_EVENT;
+    C->rng.draw = 0;
+    double tooth = orc_urand(&C->rng) * w_avg;
+    const orc_particle first = b->v[0];
+    const size_t teeth = (size_t)P->comb_teeth;
+    double sum = 0.0;
+    size_t j = 0;
+    for (size_t i = 0; i < b->n; ++i) {
+        sum += b->v[i].wgt;
+        /* j < teeth: the reference writes past bank_tmp if rounding lets
+         * one more tooth fit under the total weight */
+        if (sum > tooth && j < teeth) {
+            b->v[j] = b->v[i];
+            b->v[j].wgt = w_avg;
+            tooth += w_avg;
+            j++;
+        }
+    }
+    while (b->n < teeth) {   /* grow to the comb's size */
+        if (stack_push(b, &first) != ORC_OK) { C->status = ORC_ERR_NOMEM; return; }
+    }
+    for (size_t k = j; k < teeth; ++k) b->v[k] = first;
+    b->n = teeth;
+    for (size_t k = 0; k < teeth; ++k) b->v[k].id = orc_child_id(walker, ORC_COMB_EVENT, (uint32_t)(k + 1));
+    C->cnt[ORC_C_COMBS]++;
+}
+
 int64_t orc_n_bins(const orc_problem *P) { return P->est_bin_off[P->n_est]; }
 
 /* Simulator::start for one cycle (handler.cpp:11-48) over a history range */
@@ -829,6 +876,7 @@ int orc_run(const orc_problem *P, uint64_t first, uint64_t n, uint64_t seed,
         while (C.bank.n > 0 && C.status == ORC_OK) {
             orc_particle q = C.bank.v[--C.bank.n];
             random_walk(&C, &q);
+            if (P->comb_teeth > 0 && C.status == ORC_OK) particle_comb(&C, q.id);
         }
         if (digest) digest[h] = C.digest;
         if (hist_out) memcpy(hist_out + h * (size_t)nb, C.hist, (size_t)nb * sizeof(double));

@@ -111,6 +111,8 @@ typedef struct orc_problem {
     const double  *src_cdf;        /* n_src+1 equal-step CDF (Source.cpp:65-72) */
     /* population control (simulator.h:90-91 defaults, overridable) */
     double wr, ws;
+    /* particle comb (setup.cpp:57-67); comb_teeth == 0: off */
+    int32_t comb_bank_max, comb_teeth;
 } orc_problem;
 
 /* counters, in order */
@@ -124,6 +126,7 @@ enum {
     ORC_C_XS_EVALS,      /* macroscopic Sigma_x(E) evaluations */
     ORC_C_FREEGAS_ITERS, /* free-gas rejection-loop iterations */
     ORC_C_NUC_LOOKUPS,   /* sum over flights of the material's nuclide count */
+    ORC_C_COMBS,         /* particle-comb passes over the bank */
     ORC_C_N
 };
 

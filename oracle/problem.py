@@ -36,9 +36,9 @@ F_SURFACE, F_CELL, F_ENERGY, F_TIME, F_GROUP = range(5)
 D_DELTA, D_ISO, D_XYZ, D_HEMI_X = range(4)
 E_DELTA, E_UNIFORM = range(2)
 NUC_TABLE, NUC_CONST = range(2)
-N_COUNTERS = 9
+N_COUNTERS = 10
 COUNTER_NAMES = ["flights", "collisions", "crossings", "tally_updates", "particles",
-                 "splits", "xs_evals", "freegas_iters", "nuc_lookups"]
+                 "splits", "xs_evals", "freegas_iters", "nuc_lookups", "combs"]
 
 FLT_MAX = float(np.finfo(np.float32).max)
 
@@ -127,6 +127,7 @@ _FIELDS = [
     ("n_src", ctypes.c_int32), ("src_pos", _P), ("src_cell", _P), ("src_dir_kind", _P),
     ("src_dir_par", _P), ("src_e_kind", _P), ("src_e_par", _P), ("src_group", _P), ("src_cdf", _P),
     ("wr", ctypes.c_double), ("ws", ctypes.c_double),
+    ("comb_bank_max", ctypes.c_int32), ("comb_teeth", ctypes.c_int32),
 ]
 
 
@@ -263,10 +264,17 @@ def load(io_dir: str, xs_dir: str | None = None) -> Problem:
         raise InputError("TRMM is out of scope")
 
     wr, ws = 0.001, 1.0
+    bank_max = teeth = 0
     ctrl = doc.find("population_control")
     if ctrl is not None:
-        if ctrl.find("particle_comb") is not None:
-            raise InputError("particle comb is not supported on this path")
+        comb = ctrl.find("particle_comb")
+        if comb is not None:   # setup.cpp:57-67
+            bank_max = as_int(comb, "bank_max")
+            teeth = as_int(comb, "teeth")
+            if bank_max < 1 or teeth < 1:
+                raise InputError("particle_comb needs bank_max >= 1 and teeth >= 1")
+            if teeth > bank_max:   # the reference's history loop never ends
+                raise InputError("particle_comb with teeth > bank_max never empties the bank")
         wrn = ctrl.find("weight_roulette")
         if wrn is not None:
             wr = as_double(wrn, "wr", wr)
@@ -688,7 +696,8 @@ def load(io_dir: str, xs_dir: str | None = None) -> Problem:
     A["src_cdf"] = np.array(cdf, np.float64)
     pb.scalars = {"n_surf": len(stype), "n_cell": len(cimp), "n_mat": len(mat_lists),
                   "n_nuc": len(nuc_kind), "mg_groups": G, "n_est": len(est_names),
-                  "n_src": nsrc, "wr": wr, "ws": ws}
+                  "n_src": nsrc, "wr": wr, "ws": ws,
+                  "comb_bank_max": bank_max, "comb_teeth": teeth}
     pb.est_names = est_names
     pb.est_score_names = est_snames
     return pb

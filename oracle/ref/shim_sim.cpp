@@ -14,7 +14,9 @@
 //   2. the Philox context (history, particle id, event, draw) is advanced
 //      once per random-walk iteration, and particles copied by importance
 //      splitting get derived ids;
-//   3. wr / ws can be overridden, and a per-history event digest is kept.
+//   3. wr / ws can be overridden, and a per-history event digest is kept;
+//   4. when the input asks for the particle comb, the combed bank's copies get
+//      fresh particle ids (the comb itself is the reference's particle_comb).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -33,6 +35,9 @@ uint64_t g_shim_seed = 0x4D43;
 std::vector<uint64_t> g_shim_digest;
 
 static std::vector<uint32_t> s_ids;   // particle ids parallel to Pbank
+// the comb's draw and the combed copies' ids use this event number, which no
+// random walk reaches
+static const uint32_t kCombEvent = 0xFFFFFFFFu;
 static uint64_t s_digest;
 
 static inline void dig(uint64_t v) { s_digest = (s_digest ^ v) * 0x100000001B3ULL; }
@@ -182,6 +187,18 @@ void Simulator::start()
                 Particle P = Pbank.back(); Pbank.pop_back();
                 g_shim_rng.id = s_ids.back(); s_ids.pop_back();
                 random_walk(P);
+                if (comb) {   // handler.cpp:27, the reference's own particle_comb
+                    const uint32_t walker = g_shim_rng.id;
+                    const bool acts = Pbank.size() >= (size_t)bank_max;
+                    g_shim_rng.event = kCombEvent;
+                    g_shim_rng.draw = 0;
+                    particle_comb(Pbank);
+                    if (acts) {
+                        s_ids.resize(Pbank.size());
+                        for (size_t k = 0; k < Pbank.size(); ++k)
+                            s_ids[k] = orc_child_id(walker, kCombEvent, (uint32_t)(k + 1));
+                    }
+                }
             }
             if (tally) {
                 for (auto &E : Estimators) { E->end_history(); }

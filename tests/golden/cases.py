@@ -305,12 +305,33 @@ def absorber_slab_user_nuclides(d, samples=100_000):
     return d
 
 
+def comb_slab(d, samples=300, bank_max=3, teeth=2):
+    """slab_features with steep importances (1, 3, 9, 4, 2) and the particle
+    comb (population_control.cpp:55-84): banks of split copies reach
+    bank_max often, so the comb acts many times per history."""
+    slab_features(d, samples)
+    path = os.path.join(d, "input.xml")
+    with open(path) as f:
+        xml = f.read()
+    for name, old, new in [("r1", "2.0", "3.0"), ("r2", "4.0", "9.0"), ("r3", "2.5", "4.0"), ("r4", "1.0", "2.0")]:
+        a = '<cell name="%s" material' % name if name != "r3" else '<cell name="%s" importance' % name
+        i = xml.index(a)
+        j = xml.index('importance="%s"' % old, i)
+        xml = xml[:j] + 'importance="%s"' % new + xml[j + len('importance="%s"' % old):]
+    xml = xml.replace("</simulation>\n", "</simulation>\n<population_control>\n"
+                      '    <particle_comb bank_max="%d" teeth="%d"/>\n</population_control>\n' % (bank_max, teeth), 1)
+    with open(path, "w") as f:
+        f.write(xml)
+    return d
+
+
 # cases the compiled reference can run, with their golden-file names
 REFERENCE_CASES = {
     "ce_sphere_small": ce_sphere_small,
     "slab_features": slab_features,
     "quadrics": quadrics,
     "absorber_slab": absorber_slab,
+    "comb_slab": comb_slab,
 }
 
 

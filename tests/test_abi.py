@@ -59,7 +59,10 @@ BAD_INPUTS = {
     "fission": None,
     "unknown material": '<cells><cell name="c" material="nope"/></cells>',
     "ksearch": '<simulation><description samples="10"/><ksearch active_cycles="1" passive_cycles="1"/></simulation>',
-    "particle comb": '<population_control><particle_comb bank_max="10" teeth="5"/></population_control>',
+    "comb teeth above bank_max": ('<simulation><description samples="10"/></simulation>'
+                                  '<population_control><particle_comb bank_max="5" teeth="10"/></population_control>'),
+    "comb without teeth": ('<simulation><description samples="10"/></simulation>'
+                           '<population_control><particle_comb bank_max="5"/></population_control>'),
     "unresolved distribution": '<distributions><independentXYZ name="d" datatype="point" x="a" y="b" z="c"/></distributions>',
     "malformed xml": '<surfaces><plane_x name="p" x="1"></surfaces>',
 }
@@ -79,6 +82,8 @@ def test_input_errors_are_status_codes(L, case):
         st, msg = _load(L, d)
         assert st == 1, (st, msg)   # MC_ERR_INPUT, never an exit
         assert msg
+        if case.startswith("comb"):
+            assert "particle_comb" in msg, msg
 
 
 def test_valid_input_parses_before_device_init(L):

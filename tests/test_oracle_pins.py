@@ -93,7 +93,7 @@ def _surface_problem(OP, typ, coef):
     c[:len(coef)] = coef
     pb.arrays["surf_coef"] = c
     pb.scalars = {"n_surf": 1, "n_cell": 0, "n_mat": 0, "n_nuc": 0, "mg_groups": 0, "n_est": 0,
-                  "n_src": 0, "wr": 0.001, "ws": 1.0}
+                  "n_src": 0, "wr": 0.001, "ws": 1.0, "comb_bank_max": 0, "comb_teeth": 0}
     pb.arrays["est_bin_off"] = np.zeros(1, np.int64)
     return pb
 

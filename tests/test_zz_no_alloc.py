@@ -33,7 +33,7 @@ def mc():
     return mcgpu
 
 
-@pytest.mark.parametrize("name", ["slab_features", "ce_sphere_small"])
+@pytest.mark.parametrize("name", ["slab_features", "ce_sphere_small", "comb_slab"])
 def test_noalloc_matches_mc_run_twice(mc, name):
     import torch
     L = mc.lib()
