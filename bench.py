@@ -128,6 +128,16 @@ def _measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
+def _shape(tuned):
+    """The autotuned launch shape: kernel 1 = particle tile with event queues
+    (tile particles per CTA), kernel 2 = one particle per thread."""
+    if not tuned:
+        return None
+    if tuned.get("kernel") == 2:
+        return {"kernel": "per-thread (k_track)", "blocks_per_sm": tuned["blocks_per_sm"]}
+    return {"kernel": "tile (k_event)", "tile": tuned["bank_capacity"], "blocks_per_sm": tuned["blocks_per_sm"]}
+
+
 def _ncu_traffic():
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu
     summary (profiles/), scaled to the bench workload there; None if absent."""
@@ -308,8 +318,7 @@ def gpu_arm(a):
         "dtype": {"event": "f32 tracking / f64 tallies", "plain": "f64", "replay": "f64"}[a.mode],
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "histories_per_step": H, "mode": a.mode,
-                   "launch_shape": ({"tile": tuned["bank_capacity"], "blocks_per_sm": tuned["blocks_per_sm"]}
-                                    if tuned else None),
+                   "launch_shape": _shape(tuned),
                    "l2": "flushed (256 MiB write) before every timed step; XS tables L2-resident by design",
                    "parallelism": f"dp{world} (disjoint history ranges)"},
         "fom": {"value": statistics.mean(fom) if fom else None, "unit": "1/s",
@@ -376,7 +385,7 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
             "vs_baseline": None, "dtype": "f32 tracking / f64 tallies", "data": "synthetic",
             "config": {"workload": f"batch_shields: {len(hist)} MG slab/sphere shields, {total} histories, "
                                    "one persistent launch from a CUDA graph",
-                       "launch_shape": {"tile": tuned["bank_capacity"], "blocks_per_sm": tuned["blocks_per_sm"]},
+                       "launch_shape": _shape(tuned),
                        "l2": "flushed (256 MiB write) before every timed step"},
             "batch_latency_ms": T * 1e3,
             "fom_per_problem": {"median": float(np.median(foms)), "min": float(np.min(foms)),

@@ -60,12 +60,15 @@ typedef enum {
 typedef struct {
     uint32_t block;          /* threads per block (0 = default) */
     uint32_t grid_blocks;    /* blocks, 0 = fill the GPU */
-    uint32_t stack_depth;    /* FP64 modes: split-particle stack per thread */
+    uint32_t stack_depth;    /* split-particle stack per thread: FP64 modes and the
+                                per-thread event kernel (0 = 32) */
     uint32_t chunk;          /* FP64 modes: histories per fold chunk (0 = auto) */
     uint32_t bank_capacity;  /* event mode: particles per CTA tile (0 = tuned / 512) */
     uint32_t record_digests; /* FP64 modes: keep per-history event digests */
     uint32_t blocks_per_sm;  /* event mode: 2, 3 or 4 resident CTAs per SM, which
                                 sets the register budget (0 = tuned / 4) */
+    uint32_t kernel;         /* event mode: 1 = particle tile with event queues,
+                                2 = one particle per thread, 0 = tuned / 1 */
 } mc_tune;
 
 /* Event counters and timing of the last mc_run.  The counts follow the

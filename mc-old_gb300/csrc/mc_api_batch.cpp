@@ -22,9 +22,11 @@ struct mc_batch {
 
 namespace {
 
-// Launch shapes the autotuners try: particles per CTA tile x CTAs per SM.
-struct Shape { uint32_t tile, minb; };
-const Shape kShapes[] = {{256, 4}, {512, 4}, {512, 3}, {1024, 3}, {512, 2}, {1024, 2}, {2048, 2}};
+// Launch shapes the autotuners try: the tile kernel with particles per CTA
+// tile x CTAs per SM, and the per-thread kernel with CTAs per SM.
+struct Shape { uint32_t kernel, tile, minb; };
+const Shape kShapes[] = {{1, 256, 4}, {1, 512, 4}, {1, 512, 3}, {1, 1024, 3}, {1, 512, 2}, {1, 1024, 2},
+                         {1, 2048, 2}, {2, 0, 2}, {2, 0, 3}, {2, 0, 4}};
 
 }  // namespace
 
@@ -62,6 +64,7 @@ mc_status mc_autotune(mc_problem *p, uint64_t sample, uint64_t seed, mc_tune *ou
         mc_tune t{};
         t.bank_capacity = sh.tile;
         t.blocks_per_sm = sh.minb;
+        t.kernel = sh.kernel;
         std::string e2;
         const mc_status s2 = run_event(p->t, d, 0, sample, seed, &t, e2);
         if (s2 == MC_ERR_ARG) continue;            // shape does not fit (shared memory)
@@ -79,7 +82,7 @@ mc_status mc_autotune(mc_problem *p, uint64_t sample, uint64_t seed, mc_tune *ou
     d.last = keep_last;
     cudaFree(tmp);
     if (st != MC_OK) { p->err = "autotune: " + err; return st; }
-    if (best.bank_capacity == 0) { p->err = "autotune: no launch shape fits"; return MC_ERR_ARG; }
+    if (best.kernel == 0) { p->err = "autotune: no launch shape fits"; return MC_ERR_ARG; }
     d.tuned = best;
     *out = best;
     return MC_OK;
@@ -160,6 +163,7 @@ mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double frac, mc_tune *ou
             mc_tune t{};
             t.bank_capacity = sh.tile;
             t.blocks_per_sm = sh.minb;
+            t.kernel = sh.kernel;
             std::string e2;
             const mc_status s2 = batch_run(trial, b->sms, seed, &t, none, e2);
             if (s2 == MC_ERR_ARG) continue;
@@ -171,7 +175,7 @@ mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double frac, mc_tune *ou
     batch_state_free(trial);
     cudaFree(pool);
     if (st != MC_OK) return st;
-    if (best.bank_capacity == 0) { b->err = "autotune: no launch shape fits"; return MC_ERR_ARG; }
+    if (best.kernel == 0) { b->err = "autotune: no launch shape fits"; return MC_ERR_ARG; }
     b->tuned = best;
     *out = best;
     return MC_OK;

@@ -606,16 +606,15 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
 // ---------------------------------------------------------------------------
 // Folds a finished history's row into the sums (Estimator.cpp:339-346):
 // per-CTA shared sums for one problem, the problem's global sums in a batch.
-__device__ void history_fold(Ctx &C, int hslot)
+__device__ void history_fold(Ctx &C, int hslot, int prob)
 {
     const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
     double *acc = C.A->acc + row * C.A->row_nb;
     unsigned long long *mask = C.A->mask + row * C.A->nw;
     double *gs = C.A->sum, *gq = C.A->sq;
     if (C.A->n_prob > 0) {
-        const int pr = C.T.hprob()[hslot];
-        gs = C.A->psum[pr];
-        gq = C.A->psq[pr];
+        gs = C.A->psum[prob];
+        gq = C.A->psq[prob];
     }
     for (int wi = 0; wi < C.A->nw; ++wi) {
         if (__ldcg(mask + wi) == 0ull) continue;
@@ -643,7 +642,7 @@ __device__ __forceinline__ void particle_dies(Ctx &C, int s, int hslot)
     atomicSub(C.s_nlive, 1);
     if (atomicSub(&C.T.live()[hslot], 1) == 1) {
         __threadfence_block();
-        history_fold(C, hslot);
+        history_fold(C, hslot, C.T.hprob()[hslot]);
         const int k = atomicAdd(C.s_nhfree, 1);
         C.T.hfree()[k] = hslot;
     }
@@ -767,6 +766,172 @@ __device__ void sample_source(const EvTables &V, uint64_t seed, uint64_t hist, P
     p.id = 0u;
     p.ev = 0u;
     p.prob = 0;
+}
+
+// ---------------------------------------------------------------------------
+// one event of one particle, shared by both kernels
+// ---------------------------------------------------------------------------
+// What the advance step hands to the collision or crossing step.
+struct Flight {
+    float sig;      // Sigma_t at the collision site
+    XsAt xa;        // its place on the material's union grid (CE)
+    int S, sense;   // surface to cross and the cell's sense of it
+};
+
+// general.cpp:40-83: cross section, distance to collision (draw 0 of the
+// event), nearest surface, flight and track-length tallies.  Returns 1 for a
+// collision, 2 for a crossing, 0 if the particle is lost (status set).
+__device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R, PState &p, Flight &f)
+{
+    const int m = V.cell_mat[p.cell];
+    float dcol;
+    f.sig = 0.f;
+    f.xa = XsAt{m, 0, 0.f};
+    if (m >= 0) {
+        if (V.G > 0) {
+            f.sig = macro(C, m, XT, p);
+        } else {
+            f.xa = xs_locate(V, m, p.E);
+            f.sig = xs_at(V.gT, f.xa);
+            C.cnt[C_XS]++;
+        }
+        dcol = -__logf(R.next()) / f.sig;
+    } else {
+        dcol = 0.9f * FLT_MAX;
+    }
+    float dist = kInf;
+    f.S = -1;
+    f.sense = 0;
+    for (int i = V.cell_surf_off[p.cell]; i < V.cell_surf_off[p.cell + 1]; ++i) {
+        const int sf = V.cell_surf[i];
+        const float d = surface_distance(V, sf, p, sf == p.surf);
+        if (d < dist) { dist = d; f.S = sf; f.sense = V.cell_sense[i]; }
+    }
+    const bool cross = dcol > dist;
+    if (cross && f.S < 0) {
+        atomicCAS(C.s_status, 0, DS_LOST);
+        return 0;
+    }
+    const float l = cross ? dist : dcol;
+    const float t_old = p.t;
+    p.x = fmaf(p.u, l, p.x); p.y = fmaf(p.v, l, p.y); p.z = fmaf(p.w, l, p.z);
+    float speed = 0.f;
+    if (V.has_time) {
+        speed = speed_of(p.E);
+        p.t = t_old + l / speed;
+    }
+    C.cnt[C_FLIGHTS]++;
+    if (m >= 0 && V.G == 0) C.cnt[C_NUC] += (uint32_t)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
+    for (int i = V.cell_tl_off[p.cell]; i < V.cell_tl_off[p.cell + 1]; ++i)
+        estimator_score(C, V.cell_tl[i], p, t_old, speed, l);
+    p.surf = -1;
+    return cross ? 2 : 1;
+}
+
+// general.cpp:121-163 and population_control.cpp:9-15: collision tallies,
+// implicit capture, scatter nuclide, free-gas scatter (or multigroup
+// transfer), weight roulette.  R continues the event's stream after the
+// distance draw.  Returns whether the particle lives on.
+__device__ __forceinline__ bool event_collide(Ctx &C, const EvTables &V, Rng32 &R, PState &p, const Flight &f)
+{
+    C.cnt[C_COLL]++;
+    const int m = V.cell_mat[p.cell];
+    if (m < 0) return false;
+    for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
+        estimator_score(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f);
+    const float st = f.sig;
+    if (V.G > 0) {
+        const int row = m * V.G + p.g;
+        p.wt = p.wt * (st - __ldg(V.mg_capture + row)) / st;
+        const float *cdf = V.mg_cdf + (size_t)row * V.G;
+        const float u = __ldg(cdf + V.G - 1) * R.next();
+        int gout = -1;
+        for (int g2 = 0; g2 < V.G; ++g2)
+            if (__ldg(cdf + g2) > u) { gout = g2; break; }
+        if (gout >= 0) {
+            p.g = gout;
+            const float mu = 2.f * R.next() - 1.f;
+            float nx, ny, nz;
+            scatter_direction(R, p.u, p.v, p.w, mu, nx, ny, nz);
+            p.u = nx; p.v = ny; p.w = nz;
+        }
+        C.cnt[C_XS]++;
+    } else {
+        const XsAt &a = f.xa;
+        const float sc = xs_at(V.gC, a);
+        const float ss = xs_at(V.gS, a);
+        C.cnt[C_XS] += 2;
+        p.wt = p.wt * (st - sc) / st;
+        const float u = ss * R.next();
+        float acc = 0.f;
+        int nuc = -1;
+        for (int k = V.mnuc_off[m]; k < V.mnuc_off[m + 1]; ++k) {
+            acc += xs_at(V.nucS + V.mnuc_tab[k] - V.mgrid_off[m], a);
+            if (acc > u) { nuc = V.mnuc_id[k]; break; }
+        }
+        if (nuc >= 0 && !free_gas(C, R, p, __ldg(V.nuc_A + nuc))) atomicCAS(C.s_status, 0, DS_TIMEOUT);
+    }
+    bool alive = true;
+    if (!(fabsf(p.E) <= FLT_MAX && fabsf(p.u) <= 1.5f && fabsf(p.wt) <= FLT_MAX)) {
+        atomicCAS(C.s_status, 0, DS_NAN);
+        return false;
+    }
+    weight_roulette(C, R, p, alive);
+    return alive;
+}
+
+// general.cpp:89-115 and population_control.cpp:21-49: new cell, boundary
+// condition, crossing tallies, importance roulette / splitting, weight
+// roulette.  R must stand at draw 1 of the event.  Split copies go to
+// push(p, id), which returns false when its store is full.
+template <typename Push>
+__device__ __forceinline__ bool event_cross(Ctx &C, const EvTables &V, Rng32 &R, PState &p, const Flight &f,
+                                            Push &&push)
+{
+    C.cnt[C_CROSS]++;
+    const int S = f.S;
+    const int old_cell = p.cell;
+    bool alive = true;
+    const int bc = V.surf_bc[S];
+    p.surf = S;
+    if (bc == 0) {
+        const bool pos = !(f.sense > 0);
+        const int c = cell_across(V, p, S, pos);
+        if (c < 0) { atomicCAS(C.s_status, 0, DS_LOST); alive = false; }
+        else p.cell = c;
+    } else if (bc == -1) {
+        alive = false;
+        p.wt = 0.f;
+    } else {
+        surface_reflect(V, S, p);
+    }
+    if (p.wt != 0.f) {   // a vacuum boundary kills first and scores zero (general.cpp:98-111)
+        const float speed = V.has_time ? speed_of(p.E) : 0.f;
+        for (int i = V.surf_est_off[S]; i < V.surf_est_off[S + 1]; ++i)
+            estimator_score(C, V.surf_est[i], p, p.t, speed, 0.f);
+    }
+    if (alive && p.cell != old_cell) {
+        const float Iold = V.cell_imp[old_cell], Inew = V.cell_imp[p.cell];
+        if (Inew != Iold) {
+            const float rat = Inew / Iold;
+            if (rat < 1.f) {
+                if (R.next() < rat) p.wt = p.wt / rat;
+                else alive = false;
+            } else {
+                const int n = (int)floorf(rat + R.next());
+                p.wt = p.wt / (float)n;
+                for (int k = 1; k < n; ++k) {
+                    if (!push(p, child_id(p.id, p.ev, (uint32_t)k))) {
+                        atomicCAS(C.s_status, 0, DS_OVERFLOW);
+                        break;
+                    }
+                    C.cnt[C_SPLIT]++;
+                }
+            }
+        }
+    }
+    if (alive) weight_roulette(C, R, p, alive);
+    return alive;
 }
 
 // ---------------------------------------------------------------------------
@@ -936,51 +1101,17 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                 }
                 Rng32 R;
                 R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 0u);
-                const int m = V.cell_mat[p.cell];
-                float sig = 0.f, dcol;
-                if (m >= 0) {
-                    if (V.G > 0) {
-                        sig = macro(C, m, XT, p);
-                    } else {
-                        const XsAt a = xs_locate(V, m, p.E);
-                        sig = xs_at(V.gT, a);
-                        C.cnt[C_XS]++;
-                        T.xi()[s] = a.i;
-                        T.frac()[s] = a.f;
+                Flight f;
+                kind = event_advance(C, V, R, p, f);
+                if (kind != 0) {
+                    T.xi()[s] = f.xa.i;
+                    T.frac()[s] = f.xa.f;
+                    if (R.cached) {   // the collision continues this Philox block
+                        T.b0()[s] = R.blk.x; T.b1()[s] = R.blk.y; T.b2()[s] = R.blk.z; T.b3()[s] = R.blk.w;
                     }
-                    dcol = -__logf(R.next()) / sig;
-                    T.b0()[s] = R.blk.x; T.b1()[s] = R.blk.y; T.b2()[s] = R.blk.z; T.b3()[s] = R.blk.w;
-                } else {
-                    dcol = 0.9f * FLT_MAX;
-                }
-                float dist = kInf;
-                int S = -1, sense = 0;
-                for (int i = V.cell_surf_off[p.cell]; i < V.cell_surf_off[p.cell + 1]; ++i) {
-                    const int sf = V.cell_surf[i];
-                    const float d = surface_distance(V, sf, p, sf == p.surf);
-                    if (d < dist) { dist = d; S = sf; sense = V.cell_sense[i]; }
-                }
-                const bool cross = dcol > dist;
-                const float l = cross ? dist : dcol;
-                if (!cross || S >= 0) {
-                    const float t_old = p.t;
-                    p.x = fmaf(p.u, l, p.x); p.y = fmaf(p.v, l, p.y); p.z = fmaf(p.w, l, p.z);
-                    float speed = 0.f;
-                    if (V.has_time) {
-                        speed = speed_of(p.E);
-                        p.t = t_old + l / speed;
-                    }
-                    C.cnt[C_FLIGHTS]++;
-                    if (m >= 0 && V.G == 0) C.cnt[C_NUC] += (uint32_t)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
-                    for (int i = V.cell_tl_off[p.cell]; i < V.cell_tl_off[p.cell + 1]; ++i)
-                        estimator_score(C, V.cell_tl[i], p, t_old, speed, l);
-                    p.surf = -1;
-                    kind = cross ? 2 : 1;
-                    T.gi()[s] = S;
-                    T.sense()[s] = sense;
-                    T.sig()[s] = sig;
-                } else {
-                    atomicCAS(&s_status, 0, DS_LOST);
+                    T.gi()[s] = f.S;
+                    T.sense()[s] = f.sense;
+                    T.sig()[s] = f.sig;
                 }
                 store_p(T, s, p);
             }
@@ -1001,54 +1132,12 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
             C.V = &V;
             Rng32 R;
             R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 1u);
-            C.cnt[C_COLL]++;
-            bool alive = true;
             const int m = V.cell_mat[p.cell];
             if (m >= 0) R.preload(T.b0()[s], T.b1()[s], T.b2()[s], T.b3()[s]);
-            if (m < 0) {
-                alive = false;
-            } else {
-                for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
-                    estimator_score(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f);
-                const float st = T.sig()[s];
-                if (V.G > 0) {
-                    const int row = m * V.G + p.g;
-                    p.wt = p.wt * (st - __ldg(V.mg_capture + row)) / st;
-                    const float *cdf = V.mg_cdf + (size_t)row * V.G;
-                    const float u = __ldg(cdf + V.G - 1) * R.next();
-                    int gout = -1;
-                    for (int g2 = 0; g2 < V.G; ++g2)
-                        if (__ldg(cdf + g2) > u) { gout = g2; break; }
-                    if (gout >= 0) {
-                        p.g = gout;
-                        const float mu = 2.f * R.next() - 1.f;
-                        float nx, ny, nz;
-                        scatter_direction(R, p.u, p.v, p.w, mu, nx, ny, nz);
-                        p.u = nx; p.v = ny; p.w = nz;
-                    }
-                    C.cnt[C_XS]++;
-                } else {
-                    const XsAt a{m, T.xi()[s], T.frac()[s]};
-                    const float sc = xs_at(V.gC, a);
-                    const float ss = xs_at(V.gS, a);
-                    C.cnt[C_XS] += 2;
-                    p.wt = p.wt * (st - sc) / st;
-                    const float u = ss * R.next();
-                    float acc = 0.f;
-                    int nuc = -1;
-                    for (int k = V.mnuc_off[m]; k < V.mnuc_off[m + 1]; ++k) {
-                        acc += xs_at(V.nucS + V.mnuc_tab[k] - V.mgrid_off[m], a);
-                        if (acc > u) { nuc = V.mnuc_id[k]; break; }
-                    }
-                    if (nuc >= 0 && !free_gas(C, R, p, __ldg(V.nuc_A + nuc))) atomicCAS(&s_status, 0, DS_TIMEOUT);
-                }
-            }
-            if (alive && !(fabsf(p.E) <= FLT_MAX && fabsf(p.u) <= 1.5f && fabsf(p.wt) <= FLT_MAX)) {
-                atomicCAS(&s_status, 0, DS_NAN);
-                alive = false;
-            }
-            if (alive) weight_roulette(C, R, p, alive);
-            if (alive) store_p(T, s, p);
+            Flight f;
+            f.sig = T.sig()[s];
+            f.xa = XsAt{m, T.xi()[s], T.frac()[s]};
+            if (event_collide(C, V, R, p, f)) store_p(T, s, p);
             else particle_dies(C, s, p.hslot);
         }
 
@@ -1062,56 +1151,23 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
             C.V = &V;
             Rng32 R;
             R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 1u);
-            C.cnt[C_CROSS]++;
-            const int S = T.gi()[s];
-            const int old_cell = p.cell;
-            bool alive = true;
-            const int bc = V.surf_bc[S];
-            p.surf = S;
-            if (bc == 0) {
-                const bool pos = !(T.sense()[s] > 0);
-                const int c = cell_across(V, p, S, pos);
-                if (c < 0) { atomicCAS(&s_status, 0, DS_LOST); alive = false; }
-                else p.cell = c;
-            } else if (bc == -1) {
-                alive = false;
-                p.wt = 0.f;
-            } else {
-                surface_reflect(V, S, p);
-            }
-            if (p.wt != 0.f) {   // a vacuum boundary kills first and scores zero (general.cpp:98-111)
-                const float speed = V.has_time ? speed_of(p.E) : 0.f;
-                for (int i = V.surf_est_off[S]; i < V.surf_est_off[S + 1]; ++i)
-                    estimator_score(C, V.surf_est[i], p, p.t, speed, 0.f);
-            }
-            if (alive && p.cell != old_cell) {
-                // population_control.cpp:21-49
-                const float Iold = V.cell_imp[old_cell], Inew = V.cell_imp[p.cell];
-                if (Inew != Iold) {
-                    const float rat = Inew / Iold;
-                    if (rat < 1.f) {
-                        if (R.next() < rat) p.wt = p.wt / rat;
-                        else alive = false;
-                    } else {
-                        const int n = (int)floorf(rat + R.next());
-                        p.wt = p.wt / (float)n;
-                        for (int k = 1; k < n; ++k) {
-                            const int slot = atomicAdd(&s_novf, 1);
-                            if (slot >= A.ovf_cap) { atomicCAS(&s_status, 0, DS_OVERFLOW); break; }
-                            OvfP o;
-                            o.x = p.x; o.y = p.y; o.z = p.z; o.u = p.u; o.v = p.v; o.w = p.w;
-                            o.E = p.E; o.wt = p.wt; o.t = p.t; o.cell = p.cell; o.surf = p.surf;
-                            o.hslot = p.hslot; o.g = p.g;
-                            o.id = child_id(p.id, p.ev, (uint32_t)k);
-                            ovf[slot] = o;
-                            atomicAdd(&T.live()[p.hslot], 1);
-                            C.cnt[C_SPLIT]++;
-                        }
-                    }
-                }
-            }
-            if (alive) weight_roulette(C, R, p, alive);
-            if (alive) store_p(T, s, p);
+            Flight f;
+            f.S = T.gi()[s];
+            f.sense = T.sense()[s];
+            // split copies wait in the CTA's overflow bank
+            auto push = [&](const PState &q, uint32_t cid) -> bool {
+                const int slot = atomicAdd(&s_novf, 1);
+                if (slot >= A.ovf_cap) return false;
+                OvfP o;
+                o.x = q.x; o.y = q.y; o.z = q.z; o.u = q.u; o.v = q.v; o.w = q.w;
+                o.E = q.E; o.wt = q.wt; o.t = q.t; o.cell = q.cell; o.surf = q.surf;
+                o.hslot = q.hslot; o.g = q.g;
+                o.id = cid;
+                ovf[slot] = o;
+                atomicAdd(&T.live()[q.hslot], 1);
+                return true;
+            };
+            if (event_cross(C, V, R, p, f, push)) store_p(T, s, p);
             else particle_dies(C, s, p.hslot);
         }
         __syncthreads();
@@ -1134,6 +1190,156 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     }
 }
 
+// The per-thread loop: each thread carries one particle through event after
+// event in registers (advance, then collision or crossing, with the same
+// event functions and Philox keying as k_event), keeps its history's split
+// copies on its own LIFO stack in HBM, and takes the next history from the
+// global counter with one atomic per warp.  No block barrier separates
+// events, and no particle state goes through shared memory; shared memory
+// holds only the CTA's tally sums.  A history's row is the thread's own, so
+// it is folded when the thread finishes the history.
+constexpr int kTrackBlock = 256;
+constexpr int kTrackDepth = 32;   // default split copies a thread keeps pending
+
+template <int MinB, bool kBatch>
+__global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, const EvArgs A)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_status;
+    Ctx C;
+    C.V = &V0;
+    C.A = &A;
+    C.T.base = smem;   // P = 0: only the sums
+    C.T.P = 0;
+    C.T.nsum = A.smem_sums ? V0.n_bins : 0;
+    C.s_status = &s_status;
+    C.s_novf = nullptr;
+    C.s_nlive = nullptr;
+    C.s_nhfree = nullptr;
+    for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
+    auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
+    auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
+    if (A.smem_sums)
+        for (int b = threadIdx.x; b < 2 * V0.n_bins; b += blockDim.x) C.T.ssum()[b] = 0.0;
+    if (threadIdx.x == 0) s_status = 0;
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int hslot = threadIdx.x;
+    const int depth = A.ovf_cap / kTrackBlock;
+    OvfP *stk = A.ovf + (size_t)blockIdx.x * A.ovf_cap + (size_t)threadIdx.x * depth;
+    int sp = 0;
+    bool have = false, open = false, exhausted = false;
+    PState p;
+    uint64_t hist = 0;
+    int prob = 0;
+    uint32_t walks = 0;   // particles of the current history (bounded)
+    // split copies wait on the thread's own stack
+    auto push = [&](const PState &q, uint32_t cid) -> bool {
+        if (sp >= depth) return false;
+        OvfP o;
+        o.x = q.x; o.y = q.y; o.z = q.z; o.u = q.u; o.v = q.v; o.w = q.w;
+        o.E = q.E; o.wt = q.wt; o.t = q.t; o.cell = q.cell; o.surf = q.surf;
+        o.hslot = q.hslot; o.g = q.g;
+        o.id = cid;
+        stk[sp++] = o;
+        return true;
+    };
+    for (uint32_t it = 1;; ++it) {
+        // the next particle: the history's own split copies first (LIFO, as
+        // the reference's bank), then a new history
+        if (!have && sp > 0) {
+            const OvfP o = stk[--sp];
+            p.x = o.x; p.y = o.y; p.z = o.z; p.u = o.u; p.v = o.v; p.w = o.w;
+            p.E = o.E; p.wt = o.wt; p.t = o.t; p.cell = o.cell; p.surf = o.surf;
+            p.hslot = hslot; p.g = o.g; p.id = o.id; p.ev = 0u; p.prob = prob;
+            have = true;
+            C.cnt[C_PART]++;
+            if (++walks > (1u << 24)) atomicCAS(&s_status, 0, DS_TIMEOUT);
+        }
+        if (!have && open) {
+            history_fold(C, hslot, prob);
+            open = false;
+        }
+        const bool need = !have && !exhausted;
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(A.next, (unsigned long long)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const unsigned long long gi = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+                if (gi >= A.n) {
+                    exhausted = true;
+                } else {
+                    prob = 0;
+                    hist = A.first + gi;
+                    if (kBatch) {
+                        prob = problem_of(A, gi);
+                        hist = gi - A.prefix[prob];
+                    }
+                    sample_source(tab(prob), seed_of(prob), hist, p);
+                    p.hslot = hslot;
+                    p.prob = prob;
+                    have = true;
+                    open = true;
+                    walks = 1;
+                    C.cnt[C_PART]++;
+                }
+            }
+        }
+        // the warp leaves together: when no lane has work, or on an error
+        const bool err = *(volatile int *)&s_status != 0;
+        if (__all_sync(0xffffffffu, !have) || __any_sync(0xffffffffu, err)) break;
+        if (have) {
+            const EvTables &V = tab(prob);
+            C.V = &V;
+            p.ev += 1u;
+            if (p.ev > kMaxEvents) {          // bounded walk: report, never spin
+                atomicCAS(&s_status, 0, DS_TIMEOUT);
+                p.ev = kMaxEvents;
+            }
+            Rng32 R;
+            R.init(seed_of(prob), hist, p.id, p.ev, 0u);
+            Flight f;
+            const int kind = event_advance(C, V, R, p, f);
+            if (kind == 1) {
+                have = event_collide(C, V, R, p, f);
+            } else if (kind == 2) {
+                R.draw = 1;   // the crossing draws from word 1 on, as in k_event
+                have = event_cross(C, V, R, p, f, push);
+            }
+        }
+        if ((it & 4095u) == 0) {
+            // one event adds at most 2^16 + a few to a counter: hand the
+            // 32-bit counters to the global 64-bit ones well before they wrap
+            uint32_t big = 0;
+            for (int i = 0; i < kNumCounters; ++i) big |= C.cnt[i];
+            if (big >= (1u << 30))
+                for (int i = 0; i < kNumCounters; ++i) {
+                    atomicAdd(A.counters + i, (unsigned long long)C.cnt[i]);
+                    C.cnt[i] = 0;
+                }
+        }
+    }
+
+    __syncthreads();
+    if (A.smem_sums) {
+        for (int b = threadIdx.x; b < V0.n_bins; b += blockDim.x) {
+            const double sv = C.T.ssum()[b], qv = C.T.ssq()[b];
+            if (sv != 0.0) atomicAdd(A.sum + b, sv);
+            if (qv != 0.0) atomicAdd(A.sq + b, qv);
+        }
+    }
+    if (threadIdx.x == 0 && s_status != 0) atomicCAS(A.status, 0, s_status);
+    for (int i = 0; i < kNumCounters; ++i) {
+        unsigned long long v = C.cnt[i];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0 && v) atomicAdd(A.counters + i, v);
+    }
+}
+
 size_t tile_smem_bytes(int P, long long nb_smem)
 {
     // the layout of Tile: hidx, the four-byte arrays, qc / qx, the sums
@@ -1142,8 +1348,12 @@ size_t tile_smem_bytes(int P, long long nb_smem)
 
 typedef void (*EvKernel)(const EvTables, const EvArgs);
 
-EvKernel pick_kernel(int minb, bool batch)
+EvKernel pick_kernel(int minb, bool batch, int kernel)
 {
+    if (kernel == 2) {
+        if (batch) return minb == 2 ? k_track<2, true> : (minb == 3 ? k_track<3, true> : k_track<4, true>);
+        return minb == 2 ? k_track<2, false> : (minb == 3 ? k_track<3, false> : k_track<4, false>);
+    }
     if (batch) {
         switch (minb) {
         case 2: return k_event<2, true>;
@@ -1189,6 +1399,8 @@ const EvTables &event_tables_view(const DeviceProblem &d) { return d.ev_state->d
 // Launch geometry of the event kernel for a tune (0 fields = tuned / defaults).
 struct EvLaunch {
     int block = 256, tile = 512, minb = 4, grid = 0;
+    int kernel = 1;         // 1: tile / event queues (k_event), 2: one particle per thread (k_track)
+    int ovf_cap = 0;        // split-copy slots per CTA
     size_t smem = 0;
 };
 
@@ -1196,18 +1408,29 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
                                     long long nb_smem, bool batch, EvLaunch &L, std::string &err)
 {
     L.block = (tune && tune->block) ? (int)tune->block : 256;
-    if (L.block != 256) { err = "the event kernel is built for 256-thread blocks"; return MC_ERR_ARG; }
-    L.tile = (tune && tune->bank_capacity) ? (int)tune->bank_capacity
-           : (tuned.bank_capacity ? (int)tuned.bank_capacity : 512);
-    if (L.tile < L.block || L.tile % L.block != 0 || L.tile > 4096) {
-        err = "tile (bank_capacity) must be a multiple of 256 up to 4096";
-        return MC_ERR_ARG;
-    }
+    if (L.block != 256) { err = "the event kernels are built for 256-thread blocks"; return MC_ERR_ARG; }
+    L.kernel = (tune && tune->kernel) ? (int)tune->kernel : (tuned.kernel ? (int)tuned.kernel : 1);
+    if (L.kernel < 1 || L.kernel > 2) { err = "kernel must be 1 (tile) or 2 (per thread)"; return MC_ERR_ARG; }
     L.minb = (tune && tune->blocks_per_sm) ? (int)tune->blocks_per_sm
            : (tuned.blocks_per_sm ? (int)tuned.blocks_per_sm : 4);
     if (L.minb < 2 || L.minb > 4) { err = "blocks_per_sm must be 2, 3 or 4"; return MC_ERR_ARG; }
-    L.smem = tile_smem_bytes(L.tile, nb_smem);
-    EvKernel k = pick_kernel(L.minb, batch);
+    if (L.kernel == 2) {
+        L.tile = kTrackBlock;                  // one history row per thread
+        const int depth = (tune && tune->stack_depth) ? (int)tune->stack_depth : kTrackDepth;
+        if (depth < 1 || depth > 4096) { err = "stack_depth must be 1..4096"; return MC_ERR_ARG; }
+        L.ovf_cap = kTrackBlock * depth;
+        L.smem = sizeof(double) * 2 * (size_t)nb_smem + 64;
+    } else {
+        L.tile = (tune && tune->bank_capacity) ? (int)tune->bank_capacity
+               : (tuned.bank_capacity ? (int)tuned.bank_capacity : 512);
+        if (L.tile < L.block || L.tile % L.block != 0 || L.tile > 4096) {
+            err = "tile (bank_capacity) must be a multiple of 256 up to 4096";
+            return MC_ERR_ARG;
+        }
+        L.ovf_cap = 4 * L.tile;
+        L.smem = tile_smem_bytes(L.tile, nb_smem);
+    }
+    EvKernel k = pick_kernel(L.minb, batch, L.kernel);
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem)) != cudaSuccess) {
         err = cuda_msg(e, "event kernel shared memory");
@@ -1221,7 +1444,7 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
     return MC_OK;
 }
 
-static mc_status event_scratch(EventState &S, cudaStream_t st, int grid, int tile, long long row_nb,
+static mc_status event_scratch(EventState &S, cudaStream_t st, int grid, int tile, int ovf_cap, long long row_nb,
                                std::string &err)
 {
     const int nw = (int)((row_nb + 63) / 64);
@@ -1230,7 +1453,7 @@ static mc_status event_scratch(EventState &S, cudaStream_t st, int grid, int til
     const size_t mask_bytes = rows * nw * sizeof(unsigned long long);
     const bool grow = !S.acc.ptr || S.acc.bytes < acc_bytes || S.mask.bytes < mask_bytes;
     if (!devbuf_reserve(S.acc, acc_bytes) || !devbuf_reserve(S.mask, mask_bytes) ||
-        !devbuf_reserve(S.ovf, (size_t)grid * 4 * tile * sizeof(OvfP)) ||
+        !devbuf_reserve(S.ovf, (size_t)grid * ovf_cap * sizeof(OvfP)) ||
         !devbuf_reserve(S.misc, 256 + kNumCounters * sizeof(unsigned long long))) {
         err = "cannot allocate event-engine scratch";
         return MC_ERR_NOMEM;
@@ -1269,8 +1492,7 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     EvLaunch L;
     mc_status st = event_launch_shape(d, tune, d.tuned, smem_sums ? nb : 0, false, L, err);
     if (st != MC_OK) return st;
-    const int ovf_cap = 4 * L.tile;
-    if ((st = event_scratch(S, d.stream, L.grid, L.tile, nb, err)) != MC_OK) return st;
+    if ((st = event_scratch(S, d.stream, L.grid, L.tile, L.ovf_cap, nb, err)) != MC_OK) return st;
     char *misc = static_cast<char *>(S.misc.ptr);
     cudaMemsetAsync(misc, 0, 256 + kNumCounters * sizeof(unsigned long long), d.stream);
     EvArgs A{};
@@ -1285,14 +1507,14 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     A.nw = (int)((nb + 63) / 64);
     A.row_nb = (int)nb;
     A.ovf = static_cast<OvfP *>(S.ovf.ptr);
-    A.ovf_cap = ovf_cap;
+    A.ovf_cap = L.ovf_cap;
     A.sum = d.d_sum;
     A.sq = d.d_sq;
     A.tile = L.tile;
     A.smem_sums = smem_sums ? 1 : 0;
     A.n_prob = 0;
     cudaEventRecord(d.ev[0], d.stream);
-    pick_kernel(L.minb, false)<<<L.grid, L.block, L.smem, d.stream>>>(V, A);
+    pick_kernel(L.minb, false, L.kernel)<<<L.grid, L.block, L.smem, d.stream>>>(V, A);
     cudaError_t e;
     if ((e = cudaGetLastError()) != cudaSuccess) { err = cuda_msg(e, "event kernel launch"); return MC_ERR_CUDA; }
     cudaEventRecord(d.ev[1], d.stream);
@@ -1421,9 +1643,9 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     EvLaunch L;
     mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, L, err);
     if (st != MC_OK) return st;
-    if ((st = event_scratch(b->scratch, b->stream, L.grid, L.tile, b->row_nb, err)) != MC_OK) return st;
+    if ((st = event_scratch(b->scratch, b->stream, L.grid, L.tile, L.ovf_cap, b->row_nb, err)) != MC_OK) return st;
     const bool same_shape = b->have_shape && L.grid == b->shape.grid && L.tile == b->shape.tile &&
-                            L.minb == b->shape.minb;
+                            L.minb == b->shape.minb && L.kernel == b->shape.kernel;
     for (uint32_t i = 0; i < n; ++i) b->h_seeds[i] = batch_problem_seed(seed, i);
     char *m = static_cast<char *>(b->meta.ptr);
     size_t off = 0;
@@ -1449,7 +1671,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         A.nw = (int)((b->row_nb + 63) / 64);
         A.row_nb = (int)b->row_nb;
         A.ovf = static_cast<OvfP *>(b->scratch.ovf.ptr);
-        A.ovf_cap = 4 * L.tile;
+        A.ovf_cap = L.ovf_cap;
         A.tile = L.tile;
         A.smem_sums = 0;
         A.tabs = d_tabs;
@@ -1468,7 +1690,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         }
         cudaMemcpyAsync(d_seeds, b->h_seeds, n * 8, cudaMemcpyHostToDevice, b->stream);
         cudaMemsetAsync(misc, 0, 256 + kNumCounters * sizeof(unsigned long long), b->stream);
-        pick_kernel(L.minb, true)<<<L.grid, L.block, L.smem, b->stream>>>(V0, A);
+        pick_kernel(L.minb, true, L.kernel)<<<L.grid, L.block, L.smem, b->stream>>>(V0, A);
         if ((e = cudaStreamEndCapture(b->stream, &g)) != cudaSuccess) {
             err = cuda_msg(e, "graph capture end");
             return MC_ERR_CUDA;

@@ -46,7 +46,7 @@ class Tune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("grid_blocks", ctypes.c_uint32),
                 ("stack_depth", ctypes.c_uint32), ("chunk", ctypes.c_uint32),
                 ("bank_capacity", ctypes.c_uint32), ("record_digests", ctypes.c_uint32),
-                ("blocks_per_sm", ctypes.c_uint32)]
+                ("blocks_per_sm", ctypes.c_uint32), ("kernel", ctypes.c_uint32)]
 
 
 class Counters(ctypes.Structure):

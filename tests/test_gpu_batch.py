@@ -24,14 +24,16 @@ def _problems(mc, root, n, lo=2000, hi=20000):
     return [mc.Problem(d) for d, _ in specs], [h for _, h in specs]
 
 
-def test_batch_equals_problems_run_alone(mc):
+@pytest.mark.parametrize("kernel", [1, 2])
+def test_batch_equals_problems_run_alone(mc, kernel):
     """Problem i of a batch follows the histories of a lone run with seed
-    batch_problem_seed(seed, i): same answers (summation order aside)."""
+    batch_problem_seed(seed, i): same answers (summation order aside), with
+    either event kernel in the batch."""
     seed = 777
     with tempfile.TemporaryDirectory() as root:
         probs, hist = _problems(mc, root, 24)
         b = mc.Batch(probs, hist)
-        c = b.run(seed=seed)
+        c = b.run(seed=seed, kernel=kernel)
         assert c["histories"] == sum(hist)
         assert c["launches"] == 1
         batch_res = [p.all_tallies() for p in probs]
@@ -94,7 +96,8 @@ def test_autotune_single_and_batch(mc):
         p.run(n=1000, mode="event")
         before = p.all_tallies()[2].copy()
         t = p.autotune(sample=20000)
-        assert t["bank_capacity"] in (256, 512, 1024, 2048) and t["blocks_per_sm"] in (2, 3, 4)
+        assert t["kernel"] in (1, 2) and t["blocks_per_sm"] in (2, 3, 4)
+        assert t["kernel"] == 2 or t["bank_capacity"] in (256, 512, 1024, 2048)
         assert np.array_equal(p.all_tallies()[2], before)       # tallies untouched
         assert p.histories_run() == 1000
         p.run(n=1000, first=1000, mode="event")                 # uses the tuned shape
@@ -104,7 +107,7 @@ def test_autotune_single_and_batch(mc):
         probs, hist = _problems(mc, root, 8)
         b = mc.Batch(probs, hist)
         t = b.autotune(fraction=0.05)
-        assert t["bank_capacity"] > 0
+        assert t["kernel"] in (1, 2)
         assert all(p.histories_run() == 0 for p in probs)
         b.run(seed=3)
         assert all(p.histories_run() == h for p, h in zip(probs, hist))

@@ -40,12 +40,13 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("kernel", [1, 2])
 @pytest.mark.parametrize("name", list(CASES))
-def test_event_agrees_with_fp64(mc, name):
+def test_event_agrees_with_fp64(mc, name, kernel):
     writer, n = CASES[name]
     with tempfile.TemporaryDirectory() as d:
         writer(d)
-        m1, s1, c1 = _run(mc, d, n, "event")
+        m1, s1, c1 = _run(mc, d, n, "event", kernel=kernel)
         m2, s2, c2 = _run(mc, d, n, "replay")
     assert c1["histories"] == n
     assert_agree(m1, s1, m2, s2, name)
@@ -72,14 +73,41 @@ def _ext():
     }
 
 
+@pytest.mark.parametrize("kernel", [1, 2])
 @pytest.mark.parametrize("name", ["slab_1g", "mg_deep_slab", "mg_layered_slab"])
-def test_event_agrees_with_fp64_extensions(mc, name):
+def test_event_agrees_with_fp64_extensions(mc, name, kernel):
     writer, n = _ext()[name]
     with tempfile.TemporaryDirectory() as d:
         writer(d)
-        m1, s1, c1 = _run(mc, d, n, "event")
+        m1, s1, c1 = _run(mc, d, n, "event", kernel=kernel)
         m2, s2, c2 = _run(mc, d, n, "replay")
     assert_agree(m1, s1, m2, s2, name)
+
+
+@pytest.mark.parametrize("name", ["slab_features", "ce_sphere_small", "quadrics", "mg_layered_slab"])
+def test_per_thread_kernel_follows_the_same_histories(mc, name):
+    """The per-thread kernel (k_track) runs the tile kernel's event functions
+    with the same Philox keying, so every particle follows the same track:
+    event counts are equal and the tally sums differ only by the order of
+    FP64 additions."""
+    with tempfile.TemporaryDirectory() as d:
+        if name == "mg_layered_slab":
+            import mcgpu.workloads as W
+            W.mg_layered_slab(d, samples=100)
+            xs = None
+        else:
+            cases.write_case(name, d)
+            xs = d + "/xs_library"
+        out = []
+        for kernel in (1, 2):
+            p = mc.Problem(d, xs)
+            c = p.run(n=20000, mode="event", kernel=kernel)
+            out.append((p.all_tallies()[2].copy(), c))
+            p.close()
+    (s1, c1), (s2, c2) = out
+    for k in ("flights", "collisions", "crossings", "tally_updates", "particles", "splits", "freegas_iters"):
+        assert c1[k] == c2[k], (k, c1[k], c2[k])
+    assert np.allclose(s1, s2, rtol=1e-9, atol=1e-14)
 
 
 def test_event_tiles_and_grids(mc):
@@ -92,6 +120,25 @@ def test_event_tiles_and_grids(mc):
             m, s, c = _run(mc, d, 20000, "event", bank_capacity=tile, grid_blocks=grid)
             assert c["histories"] == 20000
             assert_agree(m, s, ref[0], ref[1], f"tile {tile} grid {grid}")
+        for minb, grid in ((2, 0), (3, 5), (4, 1)):
+            m, s, c = _run(mc, d, 20000, "event", kernel=2, blocks_per_sm=minb, grid_blocks=grid)
+            assert c["histories"] == 20000
+            assert_agree(m, s, ref[0], ref[1], f"per-thread kernel, {minb} CTAs/SM, grid {grid}")
+
+
+def test_per_thread_stack_overflow_is_a_status(mc):
+    """Split copies beyond the per-thread stack report MC_ERR_OVERFLOW and the
+    handle stays usable."""
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case("slab_features", d)
+        p = mc.Problem(d, d + "/xs_library")
+        with pytest.raises(mc.McError) as e:
+            p.run(n=5000, mode="event", kernel=2, stack_depth=1)
+        assert e.value.status == 3
+        p.reset()
+        c = p.run(n=500, mode="event", kernel=2)
+        assert c["histories"] == 500
+        p.close()
 
 
 def test_event_overflow_is_a_status(mc):
