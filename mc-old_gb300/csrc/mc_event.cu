@@ -68,7 +68,6 @@ void event_state_free(EventState *s)
 
 namespace {
 
-constexpr float kPiF = 3.14159265358979f;
 constexpr float k2PiF = 6.28318530717959f;
 constexpr float kPiHalfF = 1.57079632679490f;
 constexpr float kSqrtPiF = 1.77245385090552f;
@@ -236,6 +235,7 @@ struct Ctx {
     const EvArgs *A;
     Tile T;
     uint32_t cnt[kNumCounters];   // per-thread event counters, spilled to A.counters near 2^30
+    bool own_rows;                // a history row belongs to one thread: plain read-modify-writes
     int *s_status;
     int *s_novf;
     int *s_nlive;
@@ -494,10 +494,17 @@ __device__ int filter_idx_l(const EvTables &V, int f, const PState &p, float t_o
 __device__ __forceinline__ void tally_add(Ctx &C, int hslot, int bin, double val)
 {
     const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
-    atomicAdd(C.A->acc + row * C.A->row_nb + bin, val);
+    double *a = C.A->acc + row * C.A->row_nb + bin;
     unsigned long long *mw = C.A->mask + row * C.A->nw + (bin >> 6);
     const unsigned long long bit = 1ull << (bin & 63);
-    if (!(*(volatile unsigned long long *)mw & bit)) atomicOr(mw, bit);
+    if (C.own_rows) {
+        *a += val;
+        const unsigned long long w = *mw;
+        if (!(w & bit)) *mw = w | bit;
+    } else {   // the particles of a history run on several threads
+        atomicAdd(a, val);
+        if (!(*(volatile unsigned long long *)mw & bit)) atomicOr(mw, bit);
+    }
     C.cnt[C_TALLY]++;
 }
 
@@ -617,14 +624,27 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
         gq = C.A->psq[prob];
     }
     for (int wi = 0; wi < C.A->nw; ++wi) {
-        if (__ldcg(mask + wi) == 0ull) continue;
-        unsigned long long m = atomicExch(mask + wi, 0ull);
+        unsigned long long m;
+        if (C.own_rows) {
+            m = mask[wi];
+            if (m == 0ull) continue;
+            mask[wi] = 0ull;
+        } else {
+            if (__ldcg(mask + wi) == 0ull) continue;
+            m = atomicExch(mask + wi, 0ull);
+        }
         while (m) {
             const int b = __ffsll((long long)m) - 1;
             m &= m - 1;
             const int bin = wi * 64 + b;
-            const double v = __longlong_as_double(
-                (long long)atomicExch(reinterpret_cast<unsigned long long *>(acc + bin), 0ull));
+            double v;
+            if (C.own_rows) {
+                v = acc[bin];
+                acc[bin] = 0.0;
+            } else {
+                v = __longlong_as_double(
+                    (long long)atomicExch(reinterpret_cast<unsigned long long *>(acc + bin), 0ull));
+            }
             if (C.A->smem_sums) {
                 atomicAdd(C.T.ssum() + bin, v);
                 atomicAdd(C.T.ssq() + bin, v * v);
@@ -677,30 +697,127 @@ __device__ __forceinline__ void scatter_direction(Rng32 &R, float dx, float dy, 
     ox *= r; oy *= r; oz *= r;
 }
 
-// Reaction.cpp:27-118 in FP32
-__device__ bool free_gas(Ctx &C, Rng32 &R, PState &p, float A)
+// Free-gas elastic scatter (Reaction.cpp:27-118) in FP32, in three parts so
+// that the per-thread kernel can sample the target velocity for a whole warp
+// at once.  Candidate k of a scatter draws its six numbers from two Philox
+// blocks of its own (counter word 0xC0000000 | 2k, | 2k + 1, disjoint from the
+// event's ordinary blocks), so any lane can evaluate any particle's k-th
+// candidate and the accepted one does not depend on who evaluated it.
+struct FgState { float A, mu0, speed, beta, p_g2; };
+
+__device__ __forceinline__ void free_gas_begin(Rng32 &R, const PState &p, float A, FgState &g)
 {
-    const float mu0 = 2.f * R.next() - 1.f;
-    const float speed = speed_of(p.E);
-    const float beta = sqrtf(2.0659834e-11f * A);
-    const float y = beta * speed;
-    const float p_g2 = 2.f / (2.f + kSqrtPiF * y);
-    float V, mu;
-    for (int it = 0;; ++it) {
+    g.A = A;
+    g.mu0 = 2.f * R.next() - 1.f;
+    g.speed = speed_of(p.E);
+    g.beta = sqrtf(2.0659834e-11f * A);
+    const float y = g.beta * g.speed;
+    g.p_g2 = 2.f / (2.f + kSqrtPiF * y);
+}
+
+// Reaction.cpp:48-66: target speed V and cosine mu of candidate k, and
+// whether the rejection test accepts it.  Compiled once (noinline), so the
+// sequential and the warp-cooperative samplers get the same bits.
+__device__ __noinline__ bool fg_candidate(float speed, float beta, float p_g2, uint32_t k0, uint32_t k1,
+                                          uint32_t hlo, uint32_t id, uint32_t ev, uint32_t k, float &V, float &mu)
+{
+    const U4 a = philox(0xC0000000u | (2u * k), ev, id, hlo, k0, k1);
+    const U4 b = philox(0xC0000000u | (2u * k + 1u), ev, id, hlo, k0, k1);
+    // Reaction.cpp:48-57 without the branch: the "w2" form sqrt(-ln(a b)) is
+    // the "w1" form sqrt(-ln u1 - ln u2 cos^2) with cos = 1
+    const bool w2 = u01f(a.x) < p_g2;
+    const float cv = w2 ? 1.f : __cosf(kPiHalfF * u01f(a.w));
+    const float x = sqrtf(-__logf(u01f(a.y)) - __logf(u01f(a.z)) * (cv * cv));
+    V = x / beta;
+    mu = 2.f * u01f(b.x) - 1.f;
+    const float acc = sqrtf(fmaxf(speed * speed + V * V - 2.f * speed * V * mu, 0.f)) / (speed + V);
+    return !(u01f(b.y) > acc);
+}
+
+constexpr uint32_t kFgMaxCandidates = 1u << 16;
+
+// the rejection loop, one particle at a time (tile kernel)
+__device__ __forceinline__ bool free_gas_sample(Ctx &C, const Rng32 &R, const FgState &g, float &V, float &mu)
+{
+    for (uint32_t k = 0;; ++k) {
         C.cnt[C_FREEGAS]++;
-        if (it > (1 << 16)) return false;
-        // Reaction.cpp:48-57 without the branch: the "w2" form
-        // sqrt(-ln(a b)) is the "w1" form sqrt(-ln u1 - ln u2 cos^2) with
-        // cos = 1, so a select keeps every lane of the warp on one path
-        const bool w2 = R.next() < p_g2;
-        const float u1 = R.next(), u2 = R.next(), u3 = R.next();
-        const float cv = w2 ? 1.f : __cosf(kPiHalfF * u3);
-        const float x = sqrtf(-__logf(u1) - __logf(u2) * (cv * cv));
-        V = x / beta;
-        mu = 2.f * R.next() - 1.f;
-        const float acc = sqrtf(fmaxf(speed * speed + V * V - 2.f * speed * V * mu, 0.f)) / (speed + V);
-        if (!(R.next() > acc)) break;
+        if (k >= kFgMaxCandidates) return false;
+        if (fg_candidate(g.speed, g.beta, g.p_g2, R.k0, R.k1, R.hlo, R.id, R.ev, k, V, mu)) return true;
     }
+}
+
+// position of the n-th (0-based) set bit of m; n < popc(m)
+__device__ __forceinline__ int nth_set_bit(unsigned m, int n)
+{
+    int base = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const int c = __popc((m >> base) & ((1u << w) - 1u));
+        if (n >= c) { n -= c; base += w; }
+    }
+    return base;
+}
+
+// The rejection loop for every pending lane of the warp at once; all 32
+// lanes must call it.  Each round every lane evaluates one candidate: lane L
+// works on pending particle (L mod np) at offset (L div np) past the
+// candidates that particle has already tried.  A particle takes its first
+// accepted candidate in candidate order, which is the one the sequential loop
+// accepts; a warp needs about two rounds where the sequential loop needs the
+// longest rejection chain among its lanes.
+__device__ __forceinline__ bool warp_free_gas(Ctx &C, bool pend, const Rng32 &R, const FgState &g, float &V,
+                                              float &mu)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t tried = 0;
+    for (uint32_t round = 0;; ++round) {
+        const unsigned pm = __ballot_sync(0xffffffffu, pend);
+        if (pm == 0u) return true;
+        if (round >= kFgMaxCandidates) return !pend;
+        const int np = __popc(pm);
+        const int which = lane % np, off = lane / np;
+        const int src = nth_set_bit(pm, which);
+        const float s_speed = __shfl_sync(0xffffffffu, g.speed, src);
+        const float s_beta = __shfl_sync(0xffffffffu, g.beta, src);
+        const float s_pg2 = __shfl_sync(0xffffffffu, g.p_g2, src);
+        const uint32_t s_k0 = __shfl_sync(0xffffffffu, R.k0, src);
+        const uint32_t s_k1 = __shfl_sync(0xffffffffu, R.k1, src);
+        const uint32_t s_hlo = __shfl_sync(0xffffffffu, R.hlo, src);
+        const uint32_t s_id = __shfl_sync(0xffffffffu, R.id, src);
+        const uint32_t s_ev = __shfl_sync(0xffffffffu, R.ev, src);
+        const uint32_t s_tried = __shfl_sync(0xffffffffu, tried, src);
+        float Vc, muc;
+        const bool hit = fg_candidate(s_speed, s_beta, s_pg2, s_k0, s_k1, s_hlo, s_id, s_ev,
+                                      s_tried + (uint32_t)off, Vc, muc);
+        const unsigned sm = __ballot_sync(0xffffffffu, hit);
+        int first = -1, r = 0;
+        if (pend) {
+            r = __popc(pm & ((1u << lane) - 1u));   // this particle's rank among the pending
+            for (int L = r; L < 32; L += np)
+                if ((sm >> L) & 1u) { first = L; break; }
+        }
+        const int sel = first >= 0 ? first : lane;
+        const float Vs = __shfl_sync(0xffffffffu, Vc, sel);
+        const float ms = __shfl_sync(0xffffffffu, muc, sel);
+        if (pend) {
+            if (first >= 0) {
+                tried += (uint32_t)(first / np) + 1u;
+                C.cnt[C_FREEGAS] += tried;
+                V = Vs;
+                mu = ms;
+                pend = false;
+            } else {
+                tried += (uint32_t)((32 - r + np - 1) / np);
+            }
+        }
+    }
+}
+
+// Reaction.cpp:67-118: the outgoing velocity from the accepted target
+// velocity (two scatter_direction draws from the event's stream)
+__device__ __forceinline__ void free_gas_finish(Rng32 &R, PState &p, const FgState &g, float V, float mu)
+{
+    const float A = g.A, speed = g.speed;
     float nx, ny, nz;
     scatter_direction(R, p.u, p.v, p.w, mu, nx, ny, nz);
     const float inv = 1.f / (1.f + A);
@@ -711,13 +828,12 @@ __device__ bool free_gas(Ctx &C, Rng32 &R, PState &p, float A)
     const float sc = sqrtf(cx * cx + cy * cy + cz * cz);
     const float isc = 1.f / sc;
     float dx, dy, dz;
-    scatter_direction(R, cx * isc, cy * isc, cz * isc, mu0, dx, dy, dz);
+    scatter_direction(R, cx * isc, cy * isc, cz * isc, g.mu0, dx, dy, dz);
     const float vx = sc * dx + ux, vy = sc * dy + uy, vz = sc * dz + uz;
     const float vs = sqrtf(vx * vx + vy * vy + vz * vz);
     const float ivs = 1.f / vs;
     p.E = 5.2270376e-13f * vs * vs;
     p.u = vx * ivs; p.v = vy * ivs; p.w = vz * ivs;
-    return true;
 }
 
 __device__ __forceinline__ void weight_roulette(Ctx &C, Rng32 &R, PState &p, bool &alive)
@@ -828,15 +944,18 @@ __device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R
     return cross ? 2 : 1;
 }
 
-// general.cpp:121-163 and population_control.cpp:9-15: collision tallies,
-// implicit capture, scatter nuclide, free-gas scatter (or multigroup
-// transfer), weight roulette.  R continues the event's stream after the
-// distance draw.  Returns whether the particle lives on.
-__device__ __forceinline__ bool event_collide(Ctx &C, const EvTables &V, Rng32 &R, PState &p, const Flight &f)
+// general.cpp:121-163 and population_control.cpp:9-15 in two halves around
+// the free-gas target sampling.  The first half: collision tallies, implicit
+// capture, scatter nuclide (or the multigroup transfer); R continues the
+// event's stream after the distance draw.  Returns 0 if the particle dies (a
+// void cell), 1 if it needs no target sampling, 2 if it scatters on a
+// nuclide by free gas (g holds the sampling parameters).
+__device__ __forceinline__ int event_collide_begin(Ctx &C, const EvTables &V, Rng32 &R, PState &p, const Flight &f,
+                                                   FgState &g)
 {
     C.cnt[C_COLL]++;
     const int m = V.cell_mat[p.cell];
-    if (m < 0) return false;
+    if (m < 0) return 0;
     for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
         estimator_score(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f);
     const float st = f.sig;
@@ -856,28 +975,53 @@ __device__ __forceinline__ bool event_collide(Ctx &C, const EvTables &V, Rng32 &
             p.u = nx; p.v = ny; p.w = nz;
         }
         C.cnt[C_XS]++;
-    } else {
-        const XsAt &a = f.xa;
-        const float sc = xs_at(V.gC, a);
-        const float ss = xs_at(V.gS, a);
-        C.cnt[C_XS] += 2;
-        p.wt = p.wt * (st - sc) / st;
-        const float u = ss * R.next();
-        float acc = 0.f;
-        int nuc = -1;
-        for (int k = V.mnuc_off[m]; k < V.mnuc_off[m + 1]; ++k) {
-            acc += xs_at(V.nucS + V.mnuc_tab[k] - V.mgrid_off[m], a);
-            if (acc > u) { nuc = V.mnuc_id[k]; break; }
-        }
-        if (nuc >= 0 && !free_gas(C, R, p, __ldg(V.nuc_A + nuc))) atomicCAS(C.s_status, 0, DS_TIMEOUT);
+        return 1;
     }
-    bool alive = true;
+    const XsAt &a = f.xa;
+    const float sc = xs_at(V.gC, a);
+    const float ss = xs_at(V.gS, a);
+    C.cnt[C_XS] += 2;
+    p.wt = p.wt * (st - sc) / st;
+    const float u = ss * R.next();
+    float acc = 0.f;
+    int nuc = -1;
+    for (int k = V.mnuc_off[m]; k < V.mnuc_off[m + 1]; ++k) {
+        acc += xs_at(V.nucS + V.mnuc_tab[k] - V.mgrid_off[m], a);
+        if (acc > u) { nuc = V.mnuc_id[k]; break; }
+    }
+    if (nuc < 0) return 1;   // no scatter nuclide: the reference returns without scattering
+    free_gas_begin(R, p, __ldg(V.nuc_A + nuc), g);
+    return 2;
+}
+
+// The second half: the outgoing velocity of a free-gas scatter (st == 2,
+// target velocity V, mu), the finiteness check and weight roulette.
+__device__ __forceinline__ bool event_collide_end(Ctx &C, Rng32 &R, PState &p, int st, const FgState &g, float V,
+                                                  float mu)
+{
+    if (st == 2) free_gas_finish(R, p, g, V, mu);
     if (!(fabsf(p.E) <= FLT_MAX && fabsf(p.u) <= 1.5f && fabsf(p.wt) <= FLT_MAX)) {
         atomicCAS(C.s_status, 0, DS_NAN);
         return false;
     }
+    bool alive = true;
     weight_roulette(C, R, p, alive);
     return alive;
+}
+
+// A whole collision with the sequential rejection loop (tile kernel).
+// Returns whether the particle lives on.
+__device__ __forceinline__ bool event_collide(Ctx &C, const EvTables &V, Rng32 &R, PState &p, const Flight &f)
+{
+    FgState g;
+    int st = event_collide_begin(C, V, R, p, f, g);
+    if (st == 0) return false;
+    float Vt = 0.f, mu = 0.f;
+    if (st == 2 && !free_gas_sample(C, R, g, Vt, mu)) {
+        atomicCAS(C.s_status, 0, DS_TIMEOUT);
+        st = 1;
+    }
+    return event_collide_end(C, R, p, st, g, Vt, mu);
 }
 
 // general.cpp:89-115 and population_control.cpp:21-49: new cell, boundary
@@ -987,6 +1131,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     C.s_novf = &s_novf;
     C.s_nlive = &s_nlive;
     C.s_nhfree = &s_nhfree;
+    C.own_rows = false;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
     auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
     auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
@@ -1123,22 +1268,39 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
         __syncthreads();
 
         // ---------------- collide ----------------
+        // the warp's lanes step through the queue together, so that the
+        // free-gas target sampling can share the work across the warp
         const int nqc = s_nqc;
-        for (int j = threadIdx.x; j < nqc; j += blockDim.x) {
-            const int s = T.qc()[j];
+        for (int j0 = 0; j0 < nqc; j0 += blockDim.x) {
+            const int j = j0 + threadIdx.x;
+            const bool act = j < nqc;
+            const int s = act ? T.qc()[j] : 0;
             PState p;
-            load_p(T, s, p);
-            const EvTables &V = tab(p.prob);
-            C.V = &V;
             Rng32 R;
-            R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 1u);
-            const int m = V.cell_mat[p.cell];
-            if (m >= 0) R.preload(T.b0()[s], T.b1()[s], T.b2()[s], T.b3()[s]);
-            Flight f;
-            f.sig = T.sig()[s];
-            f.xa = XsAt{m, T.xi()[s], T.frac()[s]};
-            if (event_collide(C, V, R, p, f)) store_p(T, s, p);
-            else particle_dies(C, s, p.hslot);
+            R.init(0u, 0u, 0u, 0u, 0u);
+            FgState g;
+            int cst = 0;
+            if (act) {
+                load_p(T, s, p);
+                const EvTables &V = tab(p.prob);
+                C.V = &V;
+                R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 1u);
+                const int m = V.cell_mat[p.cell];
+                if (m >= 0) R.preload(T.b0()[s], T.b1()[s], T.b2()[s], T.b3()[s]);
+                Flight f;
+                f.sig = T.sig()[s];
+                f.xa = XsAt{m, T.xi()[s], T.frac()[s]};
+                cst = event_collide_begin(C, V, R, p, f, g);
+            }
+            float Vt = 0.f, mu = 0.f;
+            if (!warp_free_gas(C, cst == 2, R, g, Vt, mu) && cst == 2) {
+                atomicCAS(&s_status, 0, DS_TIMEOUT);
+                cst = 1;
+            }
+            if (act) {
+                if (cst != 0 && event_collide_end(C, R, p, cst, g, Vt, mu)) store_p(T, s, p);
+                else particle_dies(C, s, p.hslot);
+            }
         }
 
         // ---------------- cross ----------------
@@ -1216,6 +1378,7 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
     C.s_novf = nullptr;
     C.s_nlive = nullptr;
     C.s_nhfree = nullptr;
+    C.own_rows = true;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
     auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
     auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
@@ -1292,6 +1455,11 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
         // the warp leaves together: when no lane has work, or on an error
         const bool err = *(volatile int *)&s_status != 0;
         if (__all_sync(0xffffffffu, !have) || __any_sync(0xffffffffu, err)) break;
+        Rng32 R;
+        R.init(0u, 0u, 0u, 0u, 0u);
+        Flight f;
+        FgState g;
+        int kind = 0, cst = 0;
         if (have) {
             const EvTables &V = tab(prob);
             C.V = &V;
@@ -1300,16 +1468,23 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
                 atomicCAS(&s_status, 0, DS_TIMEOUT);
                 p.ev = kMaxEvents;
             }
-            Rng32 R;
             R.init(seed_of(prob), hist, p.id, p.ev, 0u);
-            Flight f;
-            const int kind = event_advance(C, V, R, p, f);
-            if (kind == 1) {
-                have = event_collide(C, V, R, p, f);
-            } else if (kind == 2) {
-                R.draw = 1;   // the crossing draws from word 1 on, as in k_event
-                have = event_cross(C, V, R, p, f, push);
-            }
+            kind = event_advance(C, V, R, p, f);
+            if (kind == 1) cst = event_collide_begin(C, V, R, p, f, g);
+        }
+        // free-gas target velocities for the whole warp (every lane takes part)
+        float Vt = 0.f, mu = 0.f;
+        if (!warp_free_gas(C, cst == 2, R, g, Vt, mu) && cst == 2) {
+            atomicCAS(&s_status, 0, DS_TIMEOUT);
+            cst = 1;
+        }
+        if (kind == 1) {
+            have = cst != 0 && event_collide_end(C, R, p, cst, g, Vt, mu);
+        } else if (kind == 2) {
+            const EvTables &V = tab(prob);
+            C.V = &V;
+            R.draw = 1;   // the crossing draws from word 1 on, as in k_event
+            have = event_cross(C, V, R, p, f, push);
         }
         if ((it & 4095u) == 0) {
             // one event adds at most 2^16 + a few to a counter: hand the
