@@ -138,9 +138,17 @@ def _shape(tuned):
     return {"kernel": "tile (k_event)", "tile": tuned["bank_capacity"], "blocks_per_sm": tuned["blocks_per_sm"]}
 
 
+def _traffic_key(mode, tuned):
+    """Key of the dominant kernel in profiles/traffic.json."""
+    if mode != "event":
+        return mode
+    return "event:k_track" if tuned and tuned.get("kernel") == 2 else "event:k_event"
+
+
 def _ncu_traffic():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary (profiles/), scaled to the bench workload there; None if absent."""
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum)
+    of the dominant kernel on this workload, from the committed ncu capture
+    summarised in profiles/; None if absent."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
@@ -236,11 +244,21 @@ def gpu_arm(a):
         d = make_workload(tmp, a.histories)
         prob = mcgpu.Problem(d, os.path.join(d, "xs_library"))
         H = a.histories
-        tuned = prob.autotune(sample=min(H, 1_000_000), seed=SEED + 17) if a.mode == "event" else None
+        run_kw = {}
+        if a.mode != "event":
+            tuned = None
+        elif a.kernel == "auto":
+            tuned = prob.autotune(sample=min(H, 1_000_000), seed=SEED + 17)
+        else:
+            tuned = {"kernel": 1 if a.kernel == "tile" else 2, "blocks_per_sm": a.blocks_per_sm,
+                     "bank_capacity": a.tile if a.kernel == "tile" else 0}
+            run_kw = dict(kernel=tuned["kernel"], blocks_per_sm=a.blocks_per_sm)
+            if a.kernel == "tile":
+                run_kw["bank_capacity"] = a.tile
         base = rank * (a.steps + a.warmup + a.e2e_steps + 1) * H
         for w in range(a.warmup):
             prob.reset()
-            prob.run(n=H, first=base + w * H, seed=SEED, mode=a.mode)
+            prob.run(n=H, first=base + w * H, seed=SEED, mode=a.mode, **run_kw)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -254,7 +272,7 @@ def gpu_arm(a):
             flush.zero_()
             torch.cuda.synchronize()
             prob.reset()
-            c = prob.run(n=H, first=base + (a.warmup + k) * H, seed=SEED, mode=a.mode)
+            c = prob.run(n=H, first=base + (a.warmup + k) * H, seed=SEED, mode=a.mode, **run_kw)
             dev_ms += c["total_ms"]
             transport_ms += c["transport_ms"]
             launches += c["launches"]
@@ -278,7 +296,7 @@ def gpu_arm(a):
             t0 = time.perf_counter()
             prob.upload()
             prob.reset()
-            prob.run(n=H, first=base + (a.warmup + a.steps + k) * H, seed=SEED, mode=a.mode)
+            prob.run(n=H, first=base + (a.warmup + a.steps + k) * H, seed=SEED, mode=a.mode, **run_kw)
             tot = prob.all_tallies()
             e2e_t += time.perf_counter() - t0
             d2h = int(sum(x.nbytes for x in tot[2:]))
@@ -325,7 +343,7 @@ def gpu_arm(a):
                 "tally": "leakage current at r=70 cm, R after one step"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if peak else None,
-                     "traffic": traffic.get(a.mode) if traffic else None,
+                     "traffic": (traffic or {}).get(_traffic_key(a.mode, tuned)),
                      "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs",
                      "algorithmic_bytes_per_step": alg_bytes / a.steps,
                      "kernel_ms_per_step": transport_ms / a.steps},
@@ -407,6 +425,10 @@ def main():
     ap.add_argument("--workload", default="ce_sphere", choices=["ce_sphere", "batch"])
     ap.add_argument("--batch-problems", type=int, default=4096)
     ap.add_argument("--histories", type=int, default=10_000_000)
+    ap.add_argument("--kernel", default="auto", choices=["auto", "tile", "thread"],
+                    help="event mode: autotuned, or a fixed kernel (no autotuning launches; for profiling)")
+    ap.add_argument("--blocks-per-sm", type=int, default=3)
+    ap.add_argument("--tile", type=int, default=512)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-histories", type=int, default=4000)
     ap.add_argument("--ref-histories-per-proc", type=int, default=2000)

@@ -50,8 +50,11 @@ typedef enum {
     /* FP64 history-based with the GPU's native FP64 libm and a tree fold:
      * the plain double-precision GPU history path. */
     MC_FP64_PLAIN = 1,
-    /* FP32 tracking, event-based kernels over a structure-of-arrays bank with
-     * ballot/prefix-sum compacted event queues, FP64 tally accumulation. */
+    /* FP32 tracking, FP64 tally accumulation.  Two kernels: a persistent
+     * tile of particles per CTA (structure of arrays in shared memory,
+     * ballot/prefix-sum compacted collision and crossing queues), or one
+     * particle per thread in registers; both sample free-gas targets for a
+     * whole warp at once.  mc_tune.kernel or mc_autotune picks one. */
     MC_MIXED_EVENT = 2
 } mc_mode;
 
@@ -173,7 +176,8 @@ mc_status mc_report(const mc_problem *p, const char *path);
 mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first_history, uint64_t n_histories,
                                 uint64_t seed, double *d_sum, double *d_sumsq);
 
-/* Picks the event engine's launch shape (tile of particles per CTA and
+/* Picks the mixed-precision engine's kernel and launch shape (tile kernel:
+ * particles per CTA tile and resident CTAs per SM; per-thread kernel:
  * resident CTAs per SM) for this problem by timing sample_histories in each
  * candidate shape; the winner becomes the handle's default for
  * MC_MIXED_EVENT runs made with tune == NULL and is copied to *out.  The

@@ -110,7 +110,16 @@ struct EvArgs {
     int n_prob;
 };
 
-// Philox stream of one particle and event, FP32 draws (4 per block)
+// A 23-bit uniform in (0, 1) from the bits of a block that the four word
+// draws leave unused: the low 9 bits of words 0 and 1 and 5 of word 2.
+__device__ __forceinline__ float u01f_spare(const U4 &b)
+{
+    const uint32_t v = (b.x & 0x1FFu) | ((b.y & 0x1FFu) << 9) | ((b.z & 0x1Fu) << 18);
+    return ((float)v + 0.5f) * 0x1p-23f;
+}
+
+// Philox stream of one particle and event, FP32 draws: five 23-bit uniforms
+// per block (one per word from its high 23 bits, the fifth from spare low bits)
 struct Rng32 {
     uint32_t k0, k1, hlo, id, ev, draw, cached;
     U4 blk;
@@ -132,14 +141,15 @@ struct Rng32 {
     }
     __device__ __forceinline__ float next()
     {
-        const uint32_t b = draw >> 2;
+        const uint32_t b = draw / 5u;
         if (cached != b + 1) {
             blk = philox(b | 0x80000000u, ev, id, hlo, k0, k1);
             cached = b + 1;
         }
-        const uint32_t q = draw & 3u;
-        const uint32_t word = q == 0 ? blk.x : (q == 1 ? blk.y : (q == 2 ? blk.z : blk.w));
+        const uint32_t q = draw - 5u * b;
         ++draw;
+        if (q == 4u) return u01f_spare(blk);
+        const uint32_t word = q == 0 ? blk.x : (q == 1 ? blk.y : (q == 2 ? blk.z : blk.w));
         return u01f(word);
     }
 };
@@ -230,11 +240,19 @@ __device__ __forceinline__ void store_p(const Tile &T, int s, const PState &p)
     T.id()[s] = p.id; T.ev()[s] = p.ev;
 }
 
+// Per-thread event counters live in shared memory, one column per thread
+// (conflict-free), which keeps nine registers free for the transport itself.
+constexpr int kCntStride = 256;   // threads per CTA of both kernels
+struct Counters {
+    uint32_t *base;               // this thread's column
+    __device__ __forceinline__ uint32_t &operator[](int k) const { return base[k * kCntStride]; }
+};
+
 struct Ctx {
     const EvTables *V;            // tables of the particle being processed
     const EvArgs *A;
     Tile T;
-    uint32_t cnt[kNumCounters];   // per-thread event counters, spilled to A.counters near 2^30
+    Counters cnt;                 // spilled to A.counters before they reach 2^30
     bool own_rows;                // a history row belongs to one thread: plain read-modify-writes
     int *s_status;
     int *s_novf;
@@ -699,10 +717,11 @@ __device__ __forceinline__ void scatter_direction(Rng32 &R, float dx, float dy, 
 
 // Free-gas elastic scatter (Reaction.cpp:27-118) in FP32, in three parts so
 // that the per-thread kernel can sample the target velocity for a whole warp
-// at once.  Candidate k of a scatter draws its six numbers from two Philox
-// blocks of its own (counter word 0xC0000000 | 2k, | 2k + 1, disjoint from the
-// event's ordinary blocks), so any lane can evaluate any particle's k-th
-// candidate and the accepted one does not depend on who evaluated it.
+// at once.  Candidate k of a scatter draws its six numbers from a Philox
+// block of its own (counter word 0xC0000000 | k, disjoint from the event's
+// ordinary blocks), as six 21-bit uniforms, so any lane can evaluate any
+// particle's k-th candidate and the accepted one does not depend on who
+// evaluated it.
 struct FgState { float A, mu0, speed, beta, p_g2; };
 
 __device__ __forceinline__ void free_gas_begin(Rng32 &R, const PState &p, float A, FgState &g)
@@ -718,20 +737,28 @@ __device__ __forceinline__ void free_gas_begin(Rng32 &R, const PState &p, float 
 // Reaction.cpp:48-66: target speed V and cosine mu of candidate k, and
 // whether the rejection test accepts it.  Compiled once (noinline), so the
 // sequential and the warp-cooperative samplers get the same bits.
-__device__ __noinline__ bool fg_candidate(float speed, float beta, float p_g2, uint32_t k0, uint32_t k1,
+__device__ __forceinline__ bool fg_candidate(float speed, float beta, float p_g2, uint32_t k0, uint32_t k1,
                                           uint32_t hlo, uint32_t id, uint32_t ev, uint32_t k, float &V, float &mu)
 {
-    const U4 a = philox(0xC0000000u | (2u * k), ev, id, hlo, k0, k1);
-    const U4 b = philox(0xC0000000u | (2u * k + 1u), ev, id, hlo, k0, k1);
+    const U4 a = philox(0xC0000000u | k, ev, id, hlo, k0, k1);
+    // six 21-bit uniforms: the high 21 bits of each word, then two from the
+    // low bits (11 + 10, and 1 + 11 + 9)
+    const float sc = 0x1p-21f;
+    const float r0 = ((float)(a.x >> 11) + 0.5f) * sc;
+    const float r1 = ((float)(a.y >> 11) + 0.5f) * sc;
+    const float r2 = ((float)(a.z >> 11) + 0.5f) * sc;
+    const float r3 = ((float)(a.w >> 11) + 0.5f) * sc;
+    const float r4 = ((float)((a.x & 0x7FFu) | ((a.y & 0x3FFu) << 11)) + 0.5f) * sc;
+    const float r5 = ((float)(((a.y >> 10) & 1u) | ((a.z & 0x7FFu) << 1) | ((a.w & 0x1FFu) << 12)) + 0.5f) * sc;
     // Reaction.cpp:48-57 without the branch: the "w2" form sqrt(-ln(a b)) is
     // the "w1" form sqrt(-ln u1 - ln u2 cos^2) with cos = 1
-    const bool w2 = u01f(a.x) < p_g2;
-    const float cv = w2 ? 1.f : __cosf(kPiHalfF * u01f(a.w));
-    const float x = sqrtf(-__logf(u01f(a.y)) - __logf(u01f(a.z)) * (cv * cv));
+    const bool w2 = r0 < p_g2;
+    const float cv = w2 ? 1.f : __cosf(kPiHalfF * r3);
+    const float x = sqrtf(-__logf(r1) - __logf(r2) * (cv * cv));
     V = x / beta;
-    mu = 2.f * u01f(b.x) - 1.f;
+    mu = 2.f * r4 - 1.f;
     const float acc = sqrtf(fmaxf(speed * speed + V * V - 2.f * speed * V * mu, 0.f)) / (speed + V);
-    return !(u01f(b.y) > acc);
+    return !(r5 > acc);
 }
 
 constexpr uint32_t kFgMaxCandidates = 1u << 16;
@@ -964,9 +991,15 @@ __device__ __forceinline__ int event_collide_begin(Ctx &C, const EvTables &V, Rn
         p.wt = p.wt * (st - __ldg(V.mg_capture + row)) / st;
         const float *cdf = V.mg_cdf + (size_t)row * V.G;
         const float u = __ldg(cdf + V.G - 1) * R.next();
-        int gout = -1;
-        for (int g2 = 0; g2 < V.G; ++g2)
-            if (__ldg(cdf + g2) > u) { gout = g2; break; }
+        // first group whose cumulative row entry exceeds u, by bisection
+        // (the same group a linear scan finds: the row is non-decreasing)
+        int lo = 0, hi = V.G;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(cdf + mid) > u) hi = mid;
+            else lo = mid + 1;
+        }
+        const int gout = lo < V.G ? lo : -1;
         if (gout >= 0) {
             p.g = gout;
             const float mu = 2.f * R.next() - 1.f;
@@ -1132,6 +1165,8 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     C.s_nlive = &s_nlive;
     C.s_nhfree = &s_nhfree;
     C.own_rows = false;
+    __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
+    C.cnt.base = s_cnt + threadIdx.x;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
     auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
     auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
@@ -1379,6 +1414,8 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
     C.s_nlive = nullptr;
     C.s_nhfree = nullptr;
     C.own_rows = true;
+    __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
+    C.cnt.base = s_cnt + threadIdx.x;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
     auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
     auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
