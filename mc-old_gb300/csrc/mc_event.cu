@@ -157,9 +157,9 @@ struct Rng32 {
 // shared-memory tile (SoA) and per-CTA bookkeeping.  Every array is addressed
 // from the dynamic shared-memory base and the tile size P, so the tile costs
 // two registers instead of one pointer per array.  Layout (bytes):
-//   [hidx: 8P][28 four-byte arrays: 4P each][qc: 2P][qx: 2P][ssum, ssq: 8 nb each]
+//   [hidx: 8P][30 four-byte arrays: 4P each][qc: 2P][qx: 2P][ssum, ssq: 8 nb each]
 enum TileArray {
-    TA_X, TA_Y, TA_Z, TA_U, TA_V, TA_W, TA_E, TA_WT, TA_T, TA_SIG, TA_FRAC,
+    TA_X, TA_Y, TA_Z, TA_U, TA_V, TA_W, TA_E, TA_WT, TA_T, TA_SIG, TA_FRAC, TA_SS, TA_SC,
     TA_CELL, TA_SURF, TA_HS, TA_G, TA_GI, TA_SENSE, TA_PROB, TA_XI,
     TA_B0, TA_B1, TA_B2, TA_B3,          // Philox block 0 of the current event
     TA_ID, TA_EV, TA_LIVE, TA_HFREE, TA_HPROB,
@@ -185,6 +185,8 @@ struct Tile {
     __device__ __forceinline__ float *t() const { return a4<float>(TA_T); }
     __device__ __forceinline__ float *sig() const { return a4<float>(TA_SIG); }
     __device__ __forceinline__ float *frac() const { return a4<float>(TA_FRAC); }
+    __device__ __forceinline__ float *ss() const { return a4<float>(TA_SS); }
+    __device__ __forceinline__ float *sc() const { return a4<float>(TA_SC); }
     __device__ __forceinline__ int *cell() const { return a4<int>(TA_CELL); }
     __device__ __forceinline__ int *surf() const { return a4<int>(TA_SURF); }
     __device__ __forceinline__ int *hs() const { return a4<int>(TA_HS); }
@@ -254,6 +256,8 @@ struct Ctx {
     Tile T;
     Counters cnt;                 // spilled to A.counters before they reach 2^30
     bool own_rows;                // a history row belongs to one thread: plain read-modify-writes
+    bool reg_mask;                // own rows of at most 64 bins: the touched-bin mask is tmask
+    unsigned long long tmask;     // bins the thread's current history touched (reg_mask)
     int *s_status;
     int *s_novf;
     int *s_nlive;
@@ -263,23 +267,38 @@ struct Ctx {
 // ---------------------------------------------------------------------------
 // cross sections
 // ---------------------------------------------------------------------------
-struct XsAt { int m, i; float f; };
+struct XsAt { int m, i; float f; };   // material, global grid index, fraction
 
-__device__ __forceinline__ XsAt xs_locate(const EvTables &V, int m, float E)
+// Macroscopic Sigma_t, Sigma_s, Sigma_c of material m at E (XSec.cpp:9-40
+// per nuclide, summed on the union grid): the log2 bucket gives the grid
+// point at or below the bucket start, one 32-byte load brings the two rows
+// around it ({Sigma_t, Sigma_s, Sigma_c, E} each), and a bounded walk fixes
+// the rare bracket miss.  Below the grid the first row's values hold, above
+// it the last row's (the fraction is clamped), as XSTable::xs does.
+struct XsVal { XsAt at; float st, ss, sc; };
+
+__device__ __forceinline__ XsVal xs_eval(const EvTables &V, int m, float E)
 {
     const int off = V.mgrid_off[m], L = V.mgrid_len[m];
-    const float *g = V.gE + off;
-    if (E <= __ldg(g)) return XsAt{m, off, 0.f};
-    if (E >= __ldg(g + L - 1)) return XsAt{m, off + L - 2, 1.f};
+    const float4 *row = V.xrow + off;
     int b = (int)((__log2f(E) - V.bkt_lo[m]) * V.bkt_inv[m]);
     b = b < 0 ? 0 : (b >= V.bkt_n[m] ? V.bkt_n[m] - 1 : b);
     int i = __ldg(V.bkt + V.bkt_off[m] + b);
-    while (i > 0 && __ldg(g + i) > E) --i;
-    while (__ldg(g + i + 1) < E) ++i;
-    const float e0 = __ldg(g + i), e1 = __ldg(g + i + 1);
-    return XsAt{m, off + i, (E - e0) / (e1 - e0)};
+    i = i > L - 2 ? L - 2 : i;
+    float4 r0 = __ldg(row + i), r1 = __ldg(row + i + 1);
+    while (i > 0 && r0.w > E) { --i; r1 = r0; r0 = __ldg(row + i); }
+    while (i < L - 2 && r1.w < E) { ++i; r0 = r1; r1 = __ldg(row + i + 1); }
+    float f = (E - r0.w) / (r1.w - r0.w);
+    f = f < 0.f ? 0.f : (f > 1.f ? 1.f : f);
+    XsVal x;
+    x.at = XsAt{m, off + i, f};
+    x.st = fmaf(f, r1.x - r0.x, r0.x);
+    x.ss = fmaf(f, r1.y - r0.y, r0.y);
+    x.sc = fmaf(f, r1.z - r0.z, r0.z);
+    return x;
 }
 
+// one per-nuclide table on the union grid at a located energy
 __device__ __forceinline__ float xs_at(const float *tab, const XsAt &a)
 {
     const float y0 = __ldg(tab + a.i), y1 = __ldg(tab + a.i + 1);
@@ -297,8 +316,8 @@ __device__ __forceinline__ float macro(Ctx &C, int m, int which, const PState &p
         const int i = m * V.G + p.g;
         return which == XT ? __ldg(V.mg_total + i) : (which == XS ? __ldg(V.mg_scat_tot + i) : __ldg(V.mg_capture + i));
     }
-    const XsAt a = xs_locate(V, m, p.E);
-    return xs_at(which == XT ? V.gT : (which == XS ? V.gS : V.gC), a);
+    const XsVal x = xs_eval(V, m, p.E);
+    return which == XT ? x.st : (which == XS ? x.ss : x.sc);
 }
 
 // ---------------------------------------------------------------------------
@@ -515,7 +534,10 @@ __device__ __forceinline__ void tally_add(Ctx &C, int hslot, int bin, double val
     double *a = C.A->acc + row * C.A->row_nb + bin;
     unsigned long long *mw = C.A->mask + row * C.A->nw + (bin >> 6);
     const unsigned long long bit = 1ull << (bin & 63);
-    if (C.own_rows) {
+    if (C.reg_mask) {   // a reduction the thread does not wait for, and a register mask
+        atomicAdd(a, val);
+        C.tmask |= bit;
+    } else if (C.own_rows) {
         *a += val;
         const unsigned long long w = *mw;
         if (!(w & bit)) *mw = w | bit;
@@ -643,7 +665,11 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
     }
     for (int wi = 0; wi < C.A->nw; ++wi) {
         unsigned long long m;
-        if (C.own_rows) {
+        if (C.reg_mask) {
+            m = C.tmask;
+            C.tmask = 0ull;
+            if (m == 0ull) continue;
+        } else if (C.own_rows) {
             m = mask[wi];
             if (m == 0ull) continue;
             mask[wi] = 0ull;
@@ -656,10 +682,10 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
             m &= m - 1;
             const int bin = wi * 64 + b;
             double v;
-            if (C.own_rows) {
+            if (C.own_rows && !C.reg_mask) {
                 v = acc[bin];
                 acc[bin] = 0.0;
-            } else {
+            } else {   // the row was updated by reductions (or by other threads)
                 v = __longlong_as_double(
                     (long long)atomicExch(reinterpret_cast<unsigned long long *>(acc + bin), 0ull));
             }
@@ -917,6 +943,7 @@ __device__ void sample_source(const EvTables &V, uint64_t seed, uint64_t hist, P
 // What the advance step hands to the collision or crossing step.
 struct Flight {
     float sig;      // Sigma_t at the collision site
+    float ss, sc;   // Sigma_s, Sigma_c there (CE)
     XsAt xa;        // its place on the material's union grid (CE)
     int S, sense;   // surface to cross and the cell's sense of it
 };
@@ -929,13 +956,18 @@ __device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R
     const int m = V.cell_mat[p.cell];
     float dcol;
     f.sig = 0.f;
+    f.ss = 0.f;
+    f.sc = 0.f;
     f.xa = XsAt{m, 0, 0.f};
     if (m >= 0) {
         if (V.G > 0) {
             f.sig = macro(C, m, XT, p);
         } else {
-            f.xa = xs_locate(V, m, p.E);
-            f.sig = xs_at(V.gT, f.xa);
+            const XsVal x = xs_eval(V, m, p.E);
+            f.xa = x.at;
+            f.sig = x.st;
+            f.ss = x.ss;
+            f.sc = x.sc;
             C.cnt[C_XS]++;
         }
         dcol = -__logf(R.next()) / f.sig;
@@ -1011,8 +1043,7 @@ __device__ __forceinline__ int event_collide_begin(Ctx &C, const EvTables &V, Rn
         return 1;
     }
     const XsAt &a = f.xa;
-    const float sc = xs_at(V.gC, a);
-    const float ss = xs_at(V.gS, a);
+    const float sc = f.sc, ss = f.ss;   // from the advance step's rows
     C.cnt[C_XS] += 2;
     p.wt = p.wt * (st - sc) / st;
     const float u = ss * R.next();
@@ -1165,6 +1196,8 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     C.s_nlive = &s_nlive;
     C.s_nhfree = &s_nhfree;
     C.own_rows = false;
+    C.reg_mask = false;
+    C.tmask = 0ull;
     __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
     C.cnt.base = s_cnt + threadIdx.x;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
@@ -1286,6 +1319,8 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                 if (kind != 0) {
                     T.xi()[s] = f.xa.i;
                     T.frac()[s] = f.xa.f;
+                    T.ss()[s] = f.ss;
+                    T.sc()[s] = f.sc;
                     if (R.cached) {   // the collision continues this Philox block
                         T.b0()[s] = R.blk.x; T.b1()[s] = R.blk.y; T.b2()[s] = R.blk.z; T.b3()[s] = R.blk.w;
                     }
@@ -1324,6 +1359,8 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                 if (m >= 0) R.preload(T.b0()[s], T.b1()[s], T.b2()[s], T.b3()[s]);
                 Flight f;
                 f.sig = T.sig()[s];
+                f.ss = T.ss()[s];
+                f.sc = T.sc()[s];
                 f.xa = XsAt{m, T.xi()[s], T.frac()[s]};
                 cst = event_collide_begin(C, V, R, p, f, g);
             }
@@ -1414,6 +1451,8 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
     C.s_nlive = nullptr;
     C.s_nhfree = nullptr;
     C.own_rows = true;
+    C.reg_mask = A.row_nb <= 64;
+    C.tmask = 0ull;
     __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
     C.cnt.base = s_cnt + threadIdx.x;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;

@@ -111,7 +111,7 @@ bool build_event_tables(const Tables &t, EvHost &h, std::string &err)
     V.n_mat = t.n_mat();
     V.G = t.mg_groups;
     std::vector<int> mgrid_off, mgrid_len, mnuc_off(1, 0), mnuc_id, mnuc_tab, bkt_off, bkt_n, bkt;
-    std::vector<float> gE, gT, gS, gC, nucS, bkt_lo, bkt_inv;
+    std::vector<float> xrow, nucS, bkt_lo, bkt_inv;
     if (t.mg_groups == 0) {
         for (int m = 0; m < t.n_mat(); ++m) {
             std::vector<double> grid;
@@ -130,7 +130,7 @@ bool build_event_tables(const Tables &t, EvHost &h, std::string &err)
             if (grid.size() < 2) { grid = {1e-11, 1e11}; }
             if (grid.front() <= 0.0) { err = "non-positive energy grid point"; return false; }
             const int L = (int)grid.size();
-            mgrid_off.push_back((int)gE.size());
+            mgrid_off.push_back((int)(xrow.size() / 4));
             mgrid_len.push_back(L);
             for (double e : grid) {
                 double sT = 0.0, sS = 0.0, sC = 0.0;
@@ -140,10 +140,10 @@ bool build_event_tables(const Tables &t, EvHost &h, std::string &err)
                     sS += nuc_xs(t, n, t.xs_S, e) * t.mat_dens[i];
                     sC += nuc_xs(t, n, t.xs_C, e) * t.mat_dens[i];
                 }
-                gE.push_back((float)e);
-                gT.push_back((float)sT);
-                gS.push_back((float)sS);
-                gC.push_back((float)sC);
+                xrow.push_back((float)sT);
+                xrow.push_back((float)sS);
+                xrow.push_back((float)sC);
+                xrow.push_back((float)e);
             }
             for (int i = t.mat_off[m]; i < t.mat_off[m + 1]; ++i) {
                 const int n = t.mat_nuc[i];
@@ -169,7 +169,7 @@ bool build_event_tables(const Tables &t, EvHost &h, std::string &err)
         }
     }
     P.add(mgrid_off, &V.mgrid_off); P.add(mgrid_len, &V.mgrid_len);
-    P.add(gE, &V.gE); P.add(gT, &V.gT); P.add(gS, &V.gS); P.add(gC, &V.gC);
+    P.add(xrow, reinterpret_cast<const float **>(&V.xrow));
     P.add(mnuc_off, &V.mnuc_off); P.add(mnuc_id, &V.mnuc_id); P.add(mnuc_tab, &V.mnuc_tab);
     P.add(nucS, &V.nucS);
     std::vector<float> A = cast<double, float>(t.nuc_A);

@@ -17,6 +17,7 @@
 #pragma once
 
 #include <stdint.h>
+#include <vector_types.h>   // float4 (plain struct; host code builds the rows)
 
 #include <vector>
 
@@ -47,7 +48,10 @@ struct EvTables {
     // continuous-energy materials
     int n_mat;
     const int *mgrid_off, *mgrid_len; // per material
-    const float *gE, *gT, *gS, *gC;   // union grids and macroscopic tables
+    // union grid and macroscopic tables, one 16-byte row per grid point:
+    // {Sigma_t, Sigma_s, Sigma_c, E}, so that the two rows bracketing E
+    // (one 32-byte load) give the bracket check and all three values
+    const float4 *xrow;
     const int *mnuc_off;              // per material: first entry in the nuclide lists
     const int *mnuc_id;               // nuclide index (for the mass A)
     const int *mnuc_tab;              // offset of N_k sigma_s,k on the material grid
