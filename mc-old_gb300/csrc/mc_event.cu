@@ -600,6 +600,11 @@ __device__ __forceinline__ bool estimator_score_simple(Ctx &C, int e, const PSta
 }
 
 // Estimator::score (Estimator.cpp:298-336)
+// kGen compiles in the general case (time filters: one flight may cover
+// several bins, through a pair list in local memory).  Kernels built without
+// it are launched only for problems without time filters; its code would
+// otherwise cost the hot loop registers and instruction-cache room.
+template <bool kGen>
 __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, float speed, float l_in)
 {
     const EvTables &V = *C.V;
@@ -608,6 +613,10 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
         return;
     }
     if (estimator_score_simple(C, e, p, l_in)) return;
+    if constexpr (!kGen) {
+        atomicCAS(C.s_status, 0, DS_OVERFLOW);   // unreachable: the host picks the kGen kernel
+        return;
+    }
     const int f0 = V.est_filt_off[e], nf = V.est_filt_off[e + 1] - f0;
     const int s0 = V.est_score_off[e], ns = V.est_score_off[e + 1] - s0;
     const int *fac = V.est_factor + V.est_factor_off[e];
@@ -789,16 +798,6 @@ __device__ __forceinline__ bool fg_candidate(float speed, float beta, float p_g2
 
 constexpr uint32_t kFgMaxCandidates = 1u << 16;
 
-// the rejection loop, one particle at a time (tile kernel)
-__device__ __forceinline__ bool free_gas_sample(Ctx &C, const Rng32 &R, const FgState &g, float &V, float &mu)
-{
-    for (uint32_t k = 0;; ++k) {
-        C.cnt[C_FREEGAS]++;
-        if (k >= kFgMaxCandidates) return false;
-        if (fg_candidate(g.speed, g.beta, g.p_g2, R.k0, R.k1, R.hlo, R.id, R.ev, k, V, mu)) return true;
-    }
-}
-
 // position of the n-th (0-based) set bit of m; n < popc(m)
 __device__ __forceinline__ int nth_set_bit(unsigned m, int n)
 {
@@ -951,6 +950,7 @@ struct Flight {
 // general.cpp:40-83: cross section, distance to collision (draw 0 of the
 // event), nearest surface, flight and track-length tallies.  Returns 1 for a
 // collision, 2 for a crossing, 0 if the particle is lost (status set).
+template <bool kGen>
 __device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R, PState &p, Flight &f)
 {
     const int m = V.cell_mat[p.cell];
@@ -998,7 +998,7 @@ __device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R
     C.cnt[C_FLIGHTS]++;
     if (m >= 0 && V.G == 0) C.cnt[C_NUC] += (uint32_t)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
     for (int i = V.cell_tl_off[p.cell]; i < V.cell_tl_off[p.cell + 1]; ++i)
-        estimator_score(C, V.cell_tl[i], p, t_old, speed, l);
+        estimator_score<kGen>(C, V.cell_tl[i], p, t_old, speed, l);
     p.surf = -1;
     return cross ? 2 : 1;
 }
@@ -1009,6 +1009,7 @@ __device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R
 // event's stream after the distance draw.  Returns 0 if the particle dies (a
 // void cell), 1 if it needs no target sampling, 2 if it scatters on a
 // nuclide by free gas (g holds the sampling parameters).
+template <bool kGen>
 __device__ __forceinline__ int event_collide_begin(Ctx &C, const EvTables &V, Rng32 &R, PState &p, const Flight &f,
                                                    FgState &g)
 {
@@ -1016,7 +1017,7 @@ __device__ __forceinline__ int event_collide_begin(Ctx &C, const EvTables &V, Rn
     const int m = V.cell_mat[p.cell];
     if (m < 0) return 0;
     for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
-        estimator_score(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f);
+        estimator_score<kGen>(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f);
     const float st = f.sig;
     if (V.G > 0) {
         const int row = m * V.G + p.g;
@@ -1073,26 +1074,11 @@ __device__ __forceinline__ bool event_collide_end(Ctx &C, Rng32 &R, PState &p, i
     return alive;
 }
 
-// A whole collision with the sequential rejection loop (tile kernel).
-// Returns whether the particle lives on.
-__device__ __forceinline__ bool event_collide(Ctx &C, const EvTables &V, Rng32 &R, PState &p, const Flight &f)
-{
-    FgState g;
-    int st = event_collide_begin(C, V, R, p, f, g);
-    if (st == 0) return false;
-    float Vt = 0.f, mu = 0.f;
-    if (st == 2 && !free_gas_sample(C, R, g, Vt, mu)) {
-        atomicCAS(C.s_status, 0, DS_TIMEOUT);
-        st = 1;
-    }
-    return event_collide_end(C, R, p, st, g, Vt, mu);
-}
-
 // general.cpp:89-115 and population_control.cpp:21-49: new cell, boundary
 // condition, crossing tallies, importance roulette / splitting, weight
 // roulette.  R must stand at draw 1 of the event.  Split copies go to
 // push(p, id), which returns false when its store is full.
-template <typename Push>
+template <bool kGen, typename Push>
 __device__ __forceinline__ bool event_cross(Ctx &C, const EvTables &V, Rng32 &R, PState &p, const Flight &f,
                                             Push &&push)
 {
@@ -1116,7 +1102,7 @@ __device__ __forceinline__ bool event_cross(Ctx &C, const EvTables &V, Rng32 &R,
     if (p.wt != 0.f) {   // a vacuum boundary kills first and scores zero (general.cpp:98-111)
         const float speed = V.has_time ? speed_of(p.E) : 0.f;
         for (int i = V.surf_est_off[S]; i < V.surf_est_off[S + 1]; ++i)
-            estimator_score(C, V.surf_est[i], p, p.t, speed, 0.f);
+            estimator_score<kGen>(C, V.surf_est[i], p, p.t, speed, 0.f);
     }
     if (alive && p.cell != old_cell) {
         const float Iold = V.cell_imp[old_cell], Inew = V.cell_imp[p.cell];
@@ -1315,7 +1301,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                 Rng32 R;
                 R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 0u);
                 Flight f;
-                kind = event_advance(C, V, R, p, f);
+                kind = event_advance<true>(C, V, R, p, f);
                 if (kind != 0) {
                     T.xi()[s] = f.xa.i;
                     T.frac()[s] = f.xa.f;
@@ -1362,7 +1348,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                 f.ss = T.ss()[s];
                 f.sc = T.sc()[s];
                 f.xa = XsAt{m, T.xi()[s], T.frac()[s]};
-                cst = event_collide_begin(C, V, R, p, f, g);
+                cst = event_collide_begin<true>(C, V, R, p, f, g);
             }
             float Vt = 0.f, mu = 0.f;
             if (!warp_free_gas(C, cst == 2, R, g, Vt, mu) && cst == 2) {
@@ -1401,7 +1387,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                 atomicAdd(&T.live()[q.hslot], 1);
                 return true;
             };
-            if (event_cross(C, V, R, p, f, push)) store_p(T, s, p);
+            if (event_cross<true>(C, V, R, p, f, push)) store_p(T, s, p);
             else particle_dies(C, s, p.hslot);
         }
         __syncthreads();
@@ -1435,7 +1421,7 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
 constexpr int kTrackBlock = 256;
 constexpr int kTrackDepth = 32;   // default split copies a thread keeps pending
 
-template <int MinB, bool kBatch>
+template <int MinB, bool kBatch, bool kGen>
 __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, const EvArgs A)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1545,8 +1531,8 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
                 p.ev = kMaxEvents;
             }
             R.init(seed_of(prob), hist, p.id, p.ev, 0u);
-            kind = event_advance(C, V, R, p, f);
-            if (kind == 1) cst = event_collide_begin(C, V, R, p, f, g);
+            kind = event_advance<kGen>(C, V, R, p, f);
+            if (kind == 1) cst = event_collide_begin<kGen>(C, V, R, p, f, g);
         }
         // free-gas target velocities for the whole warp (every lane takes part)
         float Vt = 0.f, mu = 0.f;
@@ -1560,7 +1546,7 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
             const EvTables &V = tab(prob);
             C.V = &V;
             R.draw = 1;   // the crossing draws from word 1 on, as in k_event
-            have = event_cross(C, V, R, p, f, push);
+            have = event_cross<kGen>(C, V, R, p, f, push);
         }
         if ((it & 4095u) == 0) {
             // one event adds at most 2^16 + a few to a counter: hand the
@@ -1599,11 +1585,15 @@ size_t tile_smem_bytes(int P, long long nb_smem)
 
 typedef void (*EvKernel)(const EvTables, const EvArgs);
 
-EvKernel pick_kernel(int minb, bool batch, int kernel)
+EvKernel pick_kernel(int minb, bool batch, int kernel, bool time_filters)
 {
     if (kernel == 2) {
-        if (batch) return minb == 2 ? k_track<2, true> : (minb == 3 ? k_track<3, true> : k_track<4, true>);
-        return minb == 2 ? k_track<2, false> : (minb == 3 ? k_track<3, false> : k_track<4, false>);
+        if (time_filters) {
+            if (batch) return minb == 2 ? k_track<2, true, true> : (minb == 3 ? k_track<3, true, true> : k_track<4, true, true>);
+            return minb == 2 ? k_track<2, false, true> : (minb == 3 ? k_track<3, false, true> : k_track<4, false, true>);
+        }
+        if (batch) return minb == 2 ? k_track<2, true, false> : (minb == 3 ? k_track<3, true, false> : k_track<4, true, false>);
+        return minb == 2 ? k_track<2, false, false> : (minb == 3 ? k_track<3, false, false> : k_track<4, false, false>);
     }
     if (batch) {
         switch (minb) {
@@ -1652,12 +1642,15 @@ struct EvLaunch {
     int block = 256, tile = 512, minb = 4, grid = 0;
     int kernel = 1;         // 1: tile / event queues (k_event), 2: one particle per thread (k_track)
     int ovf_cap = 0;        // split-copy slots per CTA
+    bool time_filters = true;   // the general estimator path is compiled in
     size_t smem = 0;
 };
 
 static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune, const mc_tune &tuned,
-                                    long long nb_smem, bool batch, EvLaunch &L, std::string &err)
+                                    long long nb_smem, bool batch, bool time_filters, EvLaunch &L,
+                                    std::string &err)
 {
+    L.time_filters = time_filters;
     L.block = (tune && tune->block) ? (int)tune->block : 256;
     if (L.block != 256) { err = "the event kernels are built for 256-thread blocks"; return MC_ERR_ARG; }
     L.kernel = (tune && tune->kernel) ? (int)tune->kernel : (tuned.kernel ? (int)tuned.kernel : 1);
@@ -1681,7 +1674,7 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
         L.ovf_cap = 4 * L.tile;
         L.smem = tile_smem_bytes(L.tile, nb_smem);
     }
-    EvKernel k = pick_kernel(L.minb, batch, L.kernel);
+    EvKernel k = pick_kernel(L.minb, batch, L.kernel, L.time_filters);
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem)) != cudaSuccess) {
         err = cuda_msg(e, "event kernel shared memory");
@@ -1741,7 +1734,7 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     const long long nb = std::max<long long>(V.n_bins, 1);
     const bool smem_sums = nb <= 4096;
     EvLaunch L;
-    mc_status st = event_launch_shape(d, tune, d.tuned, smem_sums ? nb : 0, false, L, err);
+    mc_status st = event_launch_shape(d, tune, d.tuned, smem_sums ? nb : 0, false, V.has_time != 0, L, err);
     if (st != MC_OK) return st;
     if ((st = event_scratch(S, d.stream, L.grid, L.tile, L.ovf_cap, nb, err)) != MC_OK) return st;
     char *misc = static_cast<char *>(S.misc.ptr);
@@ -1765,7 +1758,7 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     A.smem_sums = smem_sums ? 1 : 0;
     A.n_prob = 0;
     cudaEventRecord(d.ev[0], d.stream);
-    pick_kernel(L.minb, false, L.kernel)<<<L.grid, L.block, L.smem, d.stream>>>(V, A);
+    pick_kernel(L.minb, false, L.kernel, L.time_filters)<<<L.grid, L.block, L.smem, d.stream>>>(V, A);
     cudaError_t e;
     if ((e = cudaGetLastError()) != cudaSuccess) { err = cuda_msg(e, "event kernel launch"); return MC_ERR_CUDA; }
     cudaEventRecord(d.ev[1], d.stream);
@@ -1813,6 +1806,7 @@ struct BatchState {
     EvLaunch shape;
     bool have_shape = false;
     bool count_histories = true;      // false for autotuning batches
+    bool any_time = false;            // some problem has a time filter
     mc_counters last{};
 };
 
@@ -1847,6 +1841,7 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
     for (uint32_t i = 0; i < n; ++i) {
         if (!event_tables_ready(*tabs[i], *probs[i], err)) { batch_state_free(b); err = "problem " + std::to_string(i) + ": " + err; return MC_ERR_INPUT; }
         views[i] = probs[i]->ev_state->dv;
+        if (views[i].has_time) b->any_time = true;
         prefix[i + 1] = prefix[i] + hist[i];
         b->hist.push_back(hist[i]);
         psum[i] = sums_to ? (*sums_to)[2 * i] : probs[i]->d_sum;
@@ -1892,7 +1887,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     DeviceProblem shape_dev;
     shape_dev.sms = device_sms;
     EvLaunch L;
-    mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, L, err);
+    mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, b->any_time, L, err);
     if (st != MC_OK) return st;
     if ((st = event_scratch(b->scratch, b->stream, L.grid, L.tile, L.ovf_cap, b->row_nb, err)) != MC_OK) return st;
     const bool same_shape = b->have_shape && L.grid == b->shape.grid && L.tile == b->shape.tile &&
@@ -1941,7 +1936,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         }
         cudaMemcpyAsync(d_seeds, b->h_seeds, n * 8, cudaMemcpyHostToDevice, b->stream);
         cudaMemsetAsync(misc, 0, 256 + kNumCounters * sizeof(unsigned long long), b->stream);
-        pick_kernel(L.minb, true, L.kernel)<<<L.grid, L.block, L.smem, b->stream>>>(V0, A);
+        pick_kernel(L.minb, true, L.kernel, L.time_filters)<<<L.grid, L.block, L.smem, b->stream>>>(V0, A);
         if ((e = cudaStreamEndCapture(b->stream, &g)) != cudaSuccess) {
             err = cuda_msg(e, "graph capture end");
             return MC_ERR_CUDA;

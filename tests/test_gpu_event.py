@@ -88,8 +88,9 @@ def test_event_agrees_with_fp64_extensions(mc, name, kernel):
 def test_per_thread_kernel_follows_the_same_histories(mc, name):
     """The per-thread kernel (k_track) runs the tile kernel's event functions
     with the same Philox keying, so every particle follows the same track:
-    event counts are equal and the tally sums differ only by the order of
-    FP64 additions."""
+    event counts are equal, and the tally sums differ only by the order of
+    FP64 additions and the last-bit rounding of FP32 scores (the two kernels
+    are compiled separately and may fuse multiply-adds differently)."""
     with tempfile.TemporaryDirectory() as d:
         if name == "mg_layered_slab":
             import mcgpu.workloads as W
@@ -107,7 +108,7 @@ def test_per_thread_kernel_follows_the_same_histories(mc, name):
     (s1, c1), (s2, c2) = out
     for k in ("flights", "collisions", "crossings", "tally_updates", "particles", "splits", "freegas_iters"):
         assert c1[k] == c2[k], (k, c1[k], c2[k])
-    assert np.allclose(s1, s2, rtol=1e-9, atol=1e-14)
+    assert np.allclose(s1, s2, rtol=1e-6, atol=1e-14)
 
 
 def test_event_tiles_and_grids(mc):
