@@ -42,6 +42,9 @@ SOURCES = [
     ("mc_lr.cpp", "host"),
     ("mc_history.cu", "fp64"),
     ("mc_event.cu", "fast"),
+    ("mc_event_ce.cu", "fast"),
+    ("mc_event_mg.cu", "fast"),
+    ("mc_event_all.cu", "fast"),
     ("mc_noalloc.cu", "fp64"),
 ]
 
