@@ -26,6 +26,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "mcgpu", "libmcgpu.so")
+EXE = os.path.join(HERE, "mcgpu", "mcgpu_run")      # MC.exe counterpart (csrc/mc_main.cpp)
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -102,6 +103,17 @@ def build(verbose: bool = False, clean: bool = False) -> str:
             print(r.stdout + r.stderr, file=sys.stderr)
         if r.returncode != 0:
             raise RuntimeError("link failed")
+    main_src = os.path.join(CSRC, "mc_main.cpp")
+    if (not os.path.exists(EXE) or os.path.getmtime(EXE) < os.path.getmtime(LIB)
+            or os.path.getmtime(EXE) < os.path.getmtime(main_src)):
+        exe = ["g++", "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), main_src,
+               "-L", os.path.dirname(LIB), "-lmcgpu", "-Wl,-rpath,$ORIGIN", "-o", EXE]
+        r = subprocess.run(exe, capture_output=True, text=True)
+        if verbose or r.returncode != 0:
+            print(" ".join(exe), file=sys.stderr)
+            print(r.stdout + r.stderr, file=sys.stderr)
+        if r.returncode != 0:
+            raise RuntimeError("driver link failed")
     return LIB
 
 

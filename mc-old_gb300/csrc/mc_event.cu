@@ -1,23 +1,28 @@
-// mc_event.cu -- mixed-precision, event-based transport engine.
+// mc_event.cu -- mixed-precision transport engine: host side (tables on the
+// device, launch shapes, scratch, single-problem runs and batches of
+// problems replayed from a CUDA graph) and the tile kernel's instantiations.
+// The device code is in mc_event_kernels.cuh.
 //
 // The reference walks one particle at a time through general.cpp:177-211.
-// Here every CTA of a persistent grid owns a tile of particles held as a
-// structure of arrays in shared memory and advances all of them one event
-// per iteration:
+// Two persistent kernels do the same walk here, with the same event
+// functions and the same random-number keying, so they follow the same
+// tracks:
 //
-//   refill   free slots take a split copy from the CTA's overflow bank (SoA
-//            in HBM) or, when that is empty, a new history from the global
-//            history counter (one atomic per CTA per iteration);
-//   advance  every live particle: cross-section lookup, distance to
-//            collision, distance to the cell's surfaces, flight, track-length
-//            tallies; the particle joins the collision or the crossing queue
-//            (warp ballot + popc prefix, one shared atomic per warp);
-//   collide  the collision queue, dense: collision tallies, implicit capture,
-//            scatter nuclide, free-gas elastic scatter (or multigroup
-//            transfer), weight roulette;
-//   cross    the crossing queue, dense: new cell, boundary condition,
-//            crossing tallies, importance roulette / splitting, weight
-//            roulette.
+//   k_track  one particle per thread, in registers: advance (cross-section
+//            lookup, distance to collision and to the cell's surfaces,
+//            flight, track-length tallies), then the collision (collision
+//            tallies, implicit capture, scatter nuclide, free-gas target
+//            sampled by the whole warp at once, weight roulette) or the
+//            crossing (new cell, boundary condition, crossing tallies,
+//            importance roulette / splitting).  Split copies wait on the
+//            thread's own stack; a thread takes the next history with one
+//            atomic per warp.  Built in flavours (continuous energy,
+//            multigroup, everything) so that each problem runs a kernel
+//            without the code it cannot use.
+//   k_event  a tile of particles per CTA as a structure of arrays in shared
+//            memory, advanced one event per iteration: refill + advance,
+//            then the collision and crossing queues (warp ballot + popc
+//            compaction), with the split copies in a per-CTA overflow bank.
 //
 // Tracking is FP32: positions, directions, energy, weight, distances and
 // cross-section interpolation.  Sphere and cylinder roots take the constant
@@ -27,12 +32,12 @@
 // reference's FLT_EPSILON nudge and all-cell search (general.cpp:94-96),
 // which FP32 positions cannot resolve: the new cell is searched among the
 // cells that list that surface with the opposite sense.  Tallies accumulate
-// in FP64: per history into L2-resident rows (one row per tile history slot,
-// with a touched-bin mask), folded into per-CTA shared sums when the
-// history's last particle dies, and into the global sums once per CTA.
-// Physics and tally semantics follow the reference line by line as the FP64
-// path does (see mc_history.cu); only the precision and the crossing logic
-// differ, so results agree statistically, not bit for bit.
+// in FP64: per history into L2-resident rows with a touched-bin mask, folded
+// into per-CTA shared sums when the history's last particle dies, and into
+// the global sums once per CTA.  Physics and tally semantics follow the
+// reference line by line as the FP64 path does (see mc_history.cu); only the
+// precision and the crossing logic differ, so results agree statistically,
+// not bit for bit.
 #include <algorithm>
 #include <cfloat>
 #include <cstring>

@@ -95,3 +95,24 @@ def test_valid_input_parses_before_device_init(L):
         assert st in (0, 2), (st, msg)
         if st == 2:
             assert "CUDA" in msg or "device" in msg
+
+
+def test_command_line_driver_usage(L):
+    """mcgpu_run (the MC.exe counterpart) is built beside the library and,
+    like Main.cpp:11-14, asks for the input directory when given none."""
+    import subprocess
+    exe = os.path.join(ROOT, "mc-old_gb300", "mcgpu", "mcgpu_run")
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert "Please provide input.xml directory" in r.stdout
+
+
+def test_command_line_driver_reports_input_errors(L):
+    import subprocess
+    exe = os.path.join(ROOT, "mc-old_gb300", "mcgpu", "mcgpu_run")
+    with tempfile.TemporaryDirectory() as d:
+        with open(os.path.join(d, "input.xml"), "w") as f:
+            f.write("<?xml version='1.0'?>\n" + BAD_INPUTS["malformed xml"] + "\n")
+        r = subprocess.run([exe, d], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 + 1, r.stdout + r.stderr      # MC_ERR_INPUT, before any device use
+    assert "[ERROR] setup" in r.stderr
