@@ -250,6 +250,8 @@ def gpu_arm(a):
         elif a.kernel == "auto":
             tuned = prob.autotune(sample=min(H, 1_000_000), seed=SEED + 17)
         else:
+            if a.blocks_per_sm is None:
+                a.blocks_per_sm = 2 if a.kernel == "tile" else 8
             tuned = {"kernel": 1 if a.kernel == "tile" else 2, "blocks_per_sm": a.blocks_per_sm,
                      "bank_capacity": a.tile if a.kernel == "tile" else 0}
             run_kw = dict(kernel=tuned["kernel"], blocks_per_sm=a.blocks_per_sm)
@@ -427,7 +429,8 @@ def main():
     ap.add_argument("--histories", type=int, default=10_000_000)
     ap.add_argument("--kernel", default="auto", choices=["auto", "tile", "thread"],
                     help="event mode: autotuned, or a fixed kernel (no autotuning launches; for profiling)")
-    ap.add_argument("--blocks-per-sm", type=int, default=3)
+    ap.add_argument("--blocks-per-sm", type=int, default=None,
+                    help="with --kernel: resident CTAs per SM (tile: 2-4, default 2; thread: 4, 6, 7, 8, default 8)")
     ap.add_argument("--tile", type=int, default=512)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-histories", type=int, default=4000)

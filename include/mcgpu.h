@@ -68,8 +68,10 @@ typedef struct {
     uint32_t chunk;          /* FP64 modes: histories per fold chunk (0 = auto) */
     uint32_t bank_capacity;  /* event mode: particles per CTA tile (0 = tuned / 512) */
     uint32_t record_digests; /* FP64 modes: keep per-history event digests */
-    uint32_t blocks_per_sm;  /* event mode: 2, 3 or 4 resident CTAs per SM, which
-                                sets the register budget (0 = tuned / 4) */
+    uint32_t blocks_per_sm;  /* event mode: resident CTAs per SM, which sets the
+                                register budget: 2, 3 or 4 for the tile kernel
+                                (256 threads), 4, 6, 7 or 8 for the per-thread
+                                kernel (128 threads); 0 = tuned / 4 / 8 */
     uint32_t kernel;         /* event mode: 1 = particle tile with event queues,
                                 2 = one particle per thread, 0 = tuned / 1 */
 } mc_tune;

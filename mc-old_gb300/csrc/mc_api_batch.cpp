@@ -26,7 +26,7 @@ namespace {
 // tile x CTAs per SM, and the per-thread kernel with CTAs per SM.
 struct Shape { uint32_t kernel, tile, minb; };
 const Shape kShapes[] = {{1, 256, 4}, {1, 512, 4}, {1, 512, 3}, {1, 1024, 3}, {1, 512, 2}, {1, 1024, 2},
-                         {1, 2048, 2}, {2, 0, 2}, {2, 0, 3}, {2, 0, 4}};
+                         {1, 2048, 2}, {2, 0, 4}, {2, 0, 6}, {2, 0, 7}, {2, 0, 8}};
 
 }  // namespace
 

@@ -142,13 +142,24 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
                                     std::string &err)
 {
     L.flavor = flavor;
-    L.block = (tune && tune->block) ? (int)tune->block : 256;
-    if (L.block != 256) { err = "the event kernels are built for 256-thread blocks"; return MC_ERR_ARG; }
     L.kernel = (tune && tune->kernel) ? (int)tune->kernel : (tuned.kernel ? (int)tuned.kernel : 1);
     if (L.kernel < 1 || L.kernel > 2) { err = "kernel must be 1 (tile) or 2 (per thread)"; return MC_ERR_ARG; }
-    L.minb = (tune && tune->blocks_per_sm) ? (int)tune->blocks_per_sm
-           : (tuned.blocks_per_sm ? (int)tuned.blocks_per_sm : 4);
-    if (L.minb < 2 || L.minb > 4) { err = "blocks_per_sm must be 2, 3 or 4"; return MC_ERR_ARG; }
+    const int block = L.kernel == 2 ? kTrackBlock : 256;
+    L.block = (tune && tune->block) ? (int)tune->block : block;
+    if (L.block != block) {
+        err = L.kernel == 2 ? "the per-thread kernel is built for 128-thread blocks"
+                            : "the tile kernel is built for 256-thread blocks";
+        return MC_ERR_ARG;
+    }
+    const bool own_minb = tune && tune->blocks_per_sm;
+    L.minb = own_minb ? (int)tune->blocks_per_sm
+           : ((tuned.blocks_per_sm && tuned.kernel == (uint32_t)L.kernel) ? (int)tuned.blocks_per_sm
+                                                                          : (L.kernel == 2 ? 8 : 4));
+    if (L.kernel == 2 ? !(L.minb == 4 || L.minb == 6 || L.minb == 7 || L.minb == 8) : (L.minb < 2 || L.minb > 4)) {
+        err = L.kernel == 2 ? "blocks_per_sm must be 4, 6, 7 or 8 for the per-thread kernel"
+                            : "blocks_per_sm must be 2, 3 or 4 for the tile kernel";
+        return MC_ERR_ARG;
+    }
     if (L.kernel == 2) {
         L.tile = kTrackBlock;                  // one history row per thread
         const int depth = (tune && tune->stack_depth) ? (int)tune->stack_depth : kTrackDepth;

@@ -65,7 +65,9 @@ enum TileArray {
 //   FL_MG   multigroup, no time filter.
 enum Flavor { FL_ALL = 0, FL_CE = 1, FL_MG = 2 };
 
-constexpr int kTrackBlock = 256;
+// 128 threads per CTA lets the register budget step through 128 / 80 / 72 /
+// 64 registers (4 / 6 / 7 / 8 CTAs per SM)
+constexpr int kTrackBlock = 128;
 constexpr uint32_t kBatchChunk = 8;   // histories a lane takes at once in a batch
 constexpr int kTrackDepth = 32;   // default split copies a thread keeps pending
 
@@ -222,7 +224,7 @@ __device__ __forceinline__ void store_p(const Tile &T, int s, const PState &p)
 
 // Per-thread event counters live in shared memory, one column per thread
 // (conflict-free), which keeps nine registers free for the transport itself.
-constexpr int kCntStride = 256;   // threads per CTA of both kernels
+constexpr int kCntStride = 256;   // at least the threads per CTA of either kernel
 struct Counters {
     uint32_t *base;               // this thread's column
     __device__ __forceinline__ uint32_t &operator[](int k) const { return base[k * kCntStride]; }
@@ -1603,8 +1605,11 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
 template <int kFl>
 EvKernel pick_track(int minb, bool batch)
 {
-    if (batch) return minb == 2 ? k_track<2, true, kFl> : (minb == 3 ? k_track<3, true, kFl> : k_track<4, true, kFl>);
-    return minb == 2 ? k_track<2, false, kFl> : (minb == 3 ? k_track<3, false, kFl> : k_track<4, false, kFl>);
+    if (batch)
+        return minb == 4 ? k_track<4, true, kFl>
+             : minb == 6 ? k_track<6, true, kFl> : minb == 7 ? k_track<7, true, kFl> : k_track<8, true, kFl>;
+    return minb == 4 ? k_track<4, false, kFl>
+         : minb == 6 ? k_track<6, false, kFl> : minb == 7 ? k_track<7, false, kFl> : k_track<8, false, kFl>;
 }
 
 }  // namespace

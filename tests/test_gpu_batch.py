@@ -96,7 +96,7 @@ def test_autotune_single_and_batch(mc):
         p.run(n=1000, mode="event")
         before = p.all_tallies()[2].copy()
         t = p.autotune(sample=20000)
-        assert t["kernel"] in (1, 2) and t["blocks_per_sm"] in (2, 3, 4)
+        assert t["kernel"] in (1, 2) and t["blocks_per_sm"] in ((2, 3, 4) if t["kernel"] == 1 else (4, 6, 7, 8))
         assert t["kernel"] == 2 or t["bank_capacity"] in (256, 512, 1024, 2048)
         assert np.array_equal(p.all_tallies()[2], before)       # tallies untouched
         assert p.histories_run() == 1000

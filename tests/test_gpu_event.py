@@ -121,7 +121,7 @@ def test_event_tiles_and_grids(mc):
             m, s, c = _run(mc, d, 20000, "event", bank_capacity=tile, grid_blocks=grid)
             assert c["histories"] == 20000
             assert_agree(m, s, ref[0], ref[1], f"tile {tile} grid {grid}")
-        for minb, grid in ((2, 0), (3, 5), (4, 1)):
+        for minb, grid in ((4, 0), (6, 5), (8, 1)):
             m, s, c = _run(mc, d, 20000, "event", kernel=2, blocks_per_sm=minb, grid_blocks=grid)
             assert c["histories"] == 20000
             assert_agree(m, s, ref[0], ref[1], f"per-thread kernel, {minb} CTAs/SM, grid {grid}")
