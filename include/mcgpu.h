@@ -94,7 +94,7 @@ typedef struct {
     double   fold_ms;         /* device time of the history fold */
     double   total_ms;        /* device time of the whole mc_run */
     uint32_t launches;        /* kernels launched by the last mc_run */
-    uint32_t iterations;      /* event mode: event-loop iterations */
+    uint32_t reserved;        /* 0 (pads the struct to 8 bytes) */
 } mc_counters;
 
 /* Replaces Simulator::Simulator(io_dir) (src/simulator/setup.cpp:30): reads

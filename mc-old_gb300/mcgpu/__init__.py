@@ -57,7 +57,7 @@ class Counters(ctypes.Structure):
                 ("nuc_lookups", ctypes.c_uint64), ("histories", ctypes.c_uint64),
                 ("transport_ms", ctypes.c_double), ("fold_ms", ctypes.c_double),
                 ("total_ms", ctypes.c_double), ("launches", ctypes.c_uint32),
-                ("iterations", ctypes.c_uint32)]
+                ("reserved", ctypes.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
