@@ -74,6 +74,9 @@ typedef struct {
                                 kernel (128 threads); 0 = tuned / 4 / 8 */
     uint32_t kernel;         /* event mode: 1 = particle tile with event queues,
                                 2 = one particle per thread, 0 = tuned / 1 */
+    uint32_t max_events;     /* events one particle may take before the run stops
+                                with MC_ERR_TIMEOUT (0 = 2^22); a small cap
+                                exercises that path on purpose */
 } mc_tune;
 
 /* Event counters and timing of the last mc_run.  The counts follow the
@@ -123,6 +126,17 @@ mc_status mc_run(mc_problem *p, uint64_t first_history, uint64_t n_histories, ui
 
 /* Zeroes the accumulated tally sums and the history count. */
 mc_status mc_reset_tallies(mc_problem *p);
+
+/* Checkpoint / resume.  mc_state_save writes the accumulated tallies (per-bin
+ * sums of history totals and of their squares), the history count and Ntrack
+ * to a flat binary file; mc_state_load puts them into a handle made from the
+ * same input (checked by a fingerprint of the problem tables), which then
+ * continues with the histories not run yet: running [0, a), saving, loading
+ * in another process and running [a, n) gives the tallies of [0, n) (bit for
+ * bit in MC_FP64_REPLAY).  No counterpart in the reference, which keeps no
+ * state between runs. */
+mc_status mc_state_save(const mc_problem *p, const char *path);
+mc_status mc_state_load(mc_problem *p, const char *path);
 
 /* Number of estimators (the reference's Estimators.size(), simulator.h:122). */
 mc_status mc_tally_count(const mc_problem *p, uint32_t *n_estimators);

@@ -126,6 +126,69 @@ mc_status mc_reset_tallies(mc_problem *p)
     return s;
 }
 
+// A problem's fingerprint for saved states: FNV-1a over the packed device
+// tables (geometry, materials, cross sections, estimators, sources).
+static uint64_t table_fingerprint(const DeviceProblem &d)
+{
+    uint64_t h = 0xCBF29CE484222325ULL;
+    const unsigned char *b = static_cast<const unsigned char *>(d.h_blob);
+    for (size_t i = 0; i < d.blob_bytes; ++i) h = (h ^ b[i]) * 0x100000001B3ULL;
+    return h;
+}
+
+static const char kStateMagic[8] = {'M', 'C', 'G', 'P', 'U', 'S', 'T', '1'};
+
+mc_status mc_state_save(const mc_problem *p, const char *path)
+{
+    if (!p || !path) return MC_ERR_ARG;
+    std::vector<double> s, q;
+    std::string err;
+    mc_status st = read_sums(p->dev, s, q, err);
+    if (st != MC_OK) { const_cast<mc_problem *>(p)->err = err; return st; }
+    const uint64_t head[4] = {(uint64_t)s.size(), p->dev.histories, p->dev.ntrack, table_fingerprint(p->dev)};
+    FILE *f = std::fopen(path, "wb");
+    if (!f) { const_cast<mc_problem *>(p)->err = std::string("cannot write ") + path; return MC_ERR_ARG; }
+    const bool ok = std::fwrite(kStateMagic, 1, 8, f) == 8 && std::fwrite(head, 8, 4, f) == 4 &&
+                    std::fwrite(s.data(), 8, s.size(), f) == s.size() &&
+                    std::fwrite(q.data(), 8, q.size(), f) == q.size();
+    if (std::fclose(f) != 0 || !ok) {
+        const_cast<mc_problem *>(p)->err = std::string("cannot write ") + path;
+        return MC_ERR_ARG;
+    }
+    return MC_OK;
+}
+
+mc_status mc_state_load(mc_problem *p, const char *path)
+{
+    if (!p || !path) return MC_ERR_ARG;
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(p, MC_ERR_INPUT, std::string("cannot read ") + path);
+    char magic[8];
+    uint64_t head[4];
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kStateMagic, 8) == 0 &&
+              std::fread(head, 8, 4, f) == 4;
+    const size_t nb = (size_t)std::max<long long>(p->dev.dt.n_bins, 1);
+    std::vector<double> s, q;
+    if (ok && head[0] == nb && head[3] == table_fingerprint(p->dev)) {
+        s.resize(nb);
+        q.resize(nb);
+        ok = std::fread(s.data(), 8, nb, f) == nb && std::fread(q.data(), 8, nb, f) == nb;
+    } else {
+        ok = false;
+    }
+    std::fclose(f);
+    if (!ok) return fail(p, MC_ERR_INPUT, std::string(path) + " is not a saved state of this problem");
+    DeviceProblem &d = p->dev;
+    cudaError_t e;
+    if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess ||
+        (e = cudaMemcpy(d.d_sum, s.data(), nb * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(d.d_sq, q.data(), nb * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(p, MC_ERR_CUDA, cuda_msg(e, "load tallies"));
+    d.histories = head[1];
+    d.ntrack = head[2];
+    return MC_OK;
+}
+
 mc_status mc_tally_count(const mc_problem *p, uint32_t *n)
 {
     if (!p || !n) return MC_ERR_ARG;

@@ -64,6 +64,7 @@ struct HistoryArgs {
     // keep their score-function weights in lr_stack
     int n_params = 0;
     double *lr_stack = nullptr;   // [threads][stack_depth][n_params]
+    uint32_t max_events = 1u << 22;   // events per particle before DS_TIMEOUT
 };
 
 constexpr int kMaxLrParams = 64;   // (Sigma_s, Sigma_a) for up to 32 materials

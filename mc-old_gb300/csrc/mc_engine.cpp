@@ -256,6 +256,7 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
         A.hist = static_cast<double *>(d.hist.ptr);
         A.stack = d.stack.ptr;
         A.stack_depth = depth;
+        if (tune && tune->max_events) A.max_events = tune->max_events;
         A.counters = d_cnt;
         A.digest = want_digest ? static_cast<unsigned long long *>(d.digest.ptr) : nullptr;
         A.status = d_status;

@@ -134,6 +134,7 @@ struct EvLaunch {
     int kernel = 1;         // 1: tile / event queues (k_event), 2: one particle per thread (k_track)
     int ovf_cap = 0;        // split-copy slots per CTA
     int flavor = FL_ALL;    // per-thread kernel flavour (FL_ALL / FL_CE / FL_MG)
+    uint32_t max_events = kMaxEvents;
     size_t smem = 0;
 };
 
@@ -246,6 +247,7 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     A.first = first;
     A.n = n;
     A.seed = seed;
+    A.max_events = (tune && tune->max_events) ? tune->max_events : kMaxEvents;
     A.next = reinterpret_cast<unsigned long long *>(misc);
     A.status = reinterpret_cast<int *>(misc + 8);
     A.counters = reinterpret_cast<unsigned long long *>(misc + 64);
@@ -401,8 +403,10 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, b->flavor, L, err);
     if (st != MC_OK) return st;
     if ((st = event_scratch(b->scratch, b->stream, L.grid, L.tile, L.ovf_cap, b->row_nb, err)) != MC_OK) return st;
+    L.max_events = (tune && tune->max_events) ? tune->max_events : kMaxEvents;
     const bool same_shape = b->have_shape && L.grid == b->shape.grid && L.tile == b->shape.tile &&
-                            L.minb == b->shape.minb && L.kernel == b->shape.kernel;
+                            L.minb == b->shape.minb && L.kernel == b->shape.kernel &&
+                            L.max_events == b->shape.max_events;
     for (uint32_t i = 0; i < n; ++i) b->h_seeds[i] = batch_problem_seed(seed, i);
     char *m = static_cast<char *>(b->meta.ptr);
     size_t off = 0;
@@ -420,6 +424,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         A.first = 0;
         A.n = b->total;
         A.seed = 0;
+        A.max_events = L.max_events;
         A.next = reinterpret_cast<unsigned long long *>(misc);
         A.status = reinterpret_cast<int *>(misc + 8);
         A.counters = reinterpret_cast<unsigned long long *>(misc + 64);

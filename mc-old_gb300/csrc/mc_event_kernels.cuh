@@ -25,6 +25,7 @@ struct OvfP {
 
 struct EvArgs {
     uint64_t first, n, seed;
+    uint32_t max_events;          // events per particle before DS_TIMEOUT
     unsigned long long *next;     // histories handed out (relative)
     double *acc;                  // [grid * tile][row_nb]
     unsigned long long *mask;     // [grid * tile][nw]
@@ -91,7 +92,7 @@ constexpr float kEpsF = FLT_EPSILON;
 constexpr float kInf = __builtin_huge_valf();
 constexpr int kMaxFilt = 8;
 constexpr int kMaxIl = 32;
-constexpr uint32_t kMaxEvents = 1u << 22;   // events of one particle before MC_ERR_TIMEOUT
+constexpr uint32_t kMaxEvents = 1u << 22;   // default events of one particle before MC_ERR_TIMEOUT
 
 enum { C_FLIGHTS = 0, C_COLL, C_CROSS, C_TALLY, C_PART, C_SPLIT, C_XS, C_FREEGAS, C_NUC };
 
@@ -1279,9 +1280,9 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
                 const EvTables &V = tab(p.prob);
                 C.V = &V;
                 p.ev += 1u;
-                if (p.ev > kMaxEvents) {          // bounded walk: report, never spin
+                if (p.ev > A.max_events) {        // bounded walk: report, never spin
                     atomicCAS(&s_status, 0, DS_TIMEOUT);
-                    p.ev = kMaxEvents;
+                    p.ev = A.max_events;
                 }
                 Rng32 R;
                 R.init(seed_of(p.prob), T.hidx()[p.hslot], p.id, p.ev, 0u);
@@ -1549,9 +1550,9 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
             const EvTables &V = tab(prob);
             C.V = &V;
             p.ev += 1u;
-            if (p.ev > kMaxEvents) {          // bounded walk: report, never spin
+            if (p.ev > A.max_events) {        // bounded walk: report, never spin
                 atomicCAS(&s_status, 0, DS_TIMEOUT);
-                p.ev = kMaxEvents;
+                p.ev = A.max_events;
             }
             R.init(seed_of(prob), hist, p.id, p.ev, 0u);
             kind = event_advance<kFl>(C, V, R, p, f);

@@ -76,6 +76,7 @@ struct Ctx {
     double S[kMaxParams];
     double *lr_stack;
     int K;                 // parameters: (Sigma_s, Sigma_a) per material
+    uint32_t max_events;   // events per particle before DS_TIMEOUT
     long long nb;          // bins; the derivative rows follow the tally row
 };
 
@@ -651,7 +652,7 @@ __device__ void random_walk(Ctx &C, PartD &p, bool digests)
     if (digests) dig(C, 0xA5A5A5A5ULL ^ p.id);
     while (p.alive && C.status == DS_OK) {
         C.rng.start_event(C.rng.event + 1);
-        if (C.rng.event > (1u << 22)) { C.status = DS_TIMEOUT; return; }   // bounded walk
+        if (C.rng.event > C.max_events) { C.status = DS_TIMEOUT; return; }   // bounded walk
         double dist = kMaxF;
         int S = -1;
         for (int i = T.cell_surf_off[p.cell]; i < T.cell_surf_off[p.cell + 1]; ++i) {
@@ -762,6 +763,7 @@ __global__ void __launch_bounds__(128) k_history_fp64(const DevTables T, const H
     Ctx C;
     C.T = &T;
     C.depth = (int)A.stack_depth;
+    C.max_events = A.max_events;
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     C.stack = reinterpret_cast<PartD *>(A.stack) + tid * A.stack_depth;
     C.status = DS_OK;

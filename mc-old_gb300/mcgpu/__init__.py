@@ -46,7 +46,8 @@ class Tune(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("grid_blocks", ctypes.c_uint32),
                 ("stack_depth", ctypes.c_uint32), ("chunk", ctypes.c_uint32),
                 ("bank_capacity", ctypes.c_uint32), ("record_digests", ctypes.c_uint32),
-                ("blocks_per_sm", ctypes.c_uint32), ("kernel", ctypes.c_uint32)]
+                ("blocks_per_sm", ctypes.c_uint32), ("kernel", ctypes.c_uint32),
+                ("max_events", ctypes.c_uint32)]
 
 
 class Counters(ctypes.Structure):
@@ -89,6 +90,8 @@ def lib() -> ctypes.CDLL:
         L.mc_nsample.argtypes = [P, ctypes.POINTER(u64)]
         L.mc_histories_run.argtypes = [P, ctypes.POINTER(u64)]
         L.mc_report.argtypes = [P, ctypes.c_char_p]
+        L.mc_state_save.argtypes = [P, ctypes.c_char_p]
+        L.mc_state_load.argtypes = [P, ctypes.c_char_p]
         L.mc_autotune.argtypes = [P, u64, u64, ctypes.POINTER(Tune)]
         L.mc_lr_params.argtypes = [P, P, u32]
         L.mc_forward.argtypes = [P, P, u64, u64, P, P]
@@ -108,7 +111,7 @@ def lib() -> ctypes.CDLL:
                   "mc_problem_table_bytes", "mc_run", "mc_reset_tallies",
                   "mc_tally_count", "mc_tally_size", "mc_estimator_name", "mc_tally_read",
                   "mc_counters_read", "mc_digests_read", "mc_nsample", "mc_histories_run",
-                  "mc_report", "mc_autotune", "mc_lr_params", "mc_forward", "mc_backward", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
+                  "mc_report", "mc_state_save", "mc_state_load", "mc_autotune", "mc_lr_params", "mc_forward", "mc_backward", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
                   "mc_batch_autotune", "mc_batch_free"):
             getattr(L, f).restype = st
         _lib = L
@@ -216,6 +219,14 @@ class Problem:
         v = ctypes.c_uint64()
         self._check(lib().mc_histories_run(self._h, ctypes.byref(v)))
         return v.value
+
+    def save_state(self, path: str):
+        """Checkpoint the accumulated tallies (include/mcgpu.h, mc_state_save)."""
+        self._check(lib().mc_state_save(self._h, path.encode()))
+
+    def load_state(self, path: str):
+        """Resume from a checkpoint of the same problem (mc_state_load)."""
+        self._check(lib().mc_state_load(self._h, path.encode()))
 
     def report(self, path: str):
         self._check(lib().mc_report(self._h, os.fsencode(path)))
