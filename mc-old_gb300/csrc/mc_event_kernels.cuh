@@ -236,9 +236,8 @@ struct Ctx {
     const EvArgs *A;
     Tile T;
     Counters cnt;                 // spilled to A.counters before they reach 2^30
-    bool own_rows;                // a history row belongs to one thread: plain read-modify-writes
-    bool reg_mask;                // own rows of at most 64 bins: the touched-bin mask is tmask
-    unsigned long long tmask;     // bins the thread's current history touched (reg_mask)
+    bool reg_mask;                // own rows of at most 128 bins: the touched-bin mask is in registers
+    unsigned long long tmask, tmask1;   // bins 0-63 / 64-127 the current history touched (reg_mask)
     int *s_status;
     int *s_novf;
     int *s_nlive;
@@ -511,20 +510,16 @@ __device__ int filter_idx_l(const EvTables &V, int f, const PState &p, float t_o
 
 __device__ __forceinline__ void tally_add(Ctx &C, int hslot, int bin, double val)
 {
+    // the value and the touched bit are reductions in L2 that the thread does
+    // not wait for; rows of at most 128 bins keep the touched bits in registers
     const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
-    double *a = C.A->acc + row * C.A->row_nb + bin;
-    unsigned long long *mw = C.A->mask + row * C.A->nw + (bin >> 6);
+    atomicAdd(C.A->acc + row * C.A->row_nb + bin, val);
     const unsigned long long bit = 1ull << (bin & 63);
-    if (C.reg_mask) {   // a reduction the thread does not wait for, and a register mask
-        atomicAdd(a, val);
-        C.tmask |= bit;
-    } else if (C.own_rows) {
-        *a += val;
-        const unsigned long long w = *mw;
-        if (!(w & bit)) *mw = w | bit;
-    } else {   // the particles of a history run on several threads
-        atomicAdd(a, val);
-        if (!(*(volatile unsigned long long *)mw & bit)) atomicOr(mw, bit);
+    if (C.reg_mask) {
+        if (bin & 64) C.tmask1 |= bit;
+        else C.tmask |= bit;
+    } else {
+        atomicOr(C.A->mask + row * C.A->nw + (bin >> 6), bit);
     }
     C.cnt[C_TALLY]++;
 }
@@ -551,18 +546,28 @@ __device__ float score_value(Ctx &C, int sc, const PState &p, float l)
 // filter: every filter yields one (bin, length) pair or none, all lengths
 // equal l_in, so the combination loop collapses to one flattened index and
 // needs no pair list (which would live in local memory).
-__device__ __forceinline__ bool estimator_score_simple(Ctx &C, int e, const PState &p, float l_in)
+//
+// pre / fixed: an estimator attached to a cell (track-length, collision) or
+// to a surface (crossing) has its cell or surface filter fixed by the
+// attachment.  The table builder resolved that filter's part of the flattened
+// index once per attachment (pre; -1: the cell or surface lies outside the
+// filter, nothing is scored), and the loop skips filters of kind `fixed`.
+__device__ __forceinline__ bool estimator_score_simple(Ctx &C, int e, const PState &p, float l_in, int pre,
+                                                       int fixed)
 {
     const EvTables &V = *C.V;
     const int f0 = V.est_filt_off[e], nf = V.est_filt_off[e + 1] - f0;
     const int *fac = V.est_factor + V.est_factor_off[e];
-    int idx1 = 0;
+    if (pre < 0) return true;
+    int idx1 = pre;
     for (int i = 0; i < nf; ++i) {
         const int f = f0 + i;
+        const int kind = V.filt_kind[f];
+        if (kind == fixed) continue;
         const float *grid = V.filt_grid + V.filt_grid_off[f];
         const int glen = V.filt_grid_len[f];
         int b;
-        switch (V.filt_kind[f]) {
+        switch (kind) {
         case 0: b = bsearch_f((float)p.surf, grid, glen) + 1; if (b < 0 || b >= V.filt_size[f]) return true; break;
         case 1: b = bsearch_f((float)p.cell, grid, glen) + 1; if (b < 0 || b >= V.filt_size[f]) return true; break;
         case 2: b = bsearch_f(p.E, grid, glen); if (b < 0 || b >= glen - 1) return true; break;
@@ -580,8 +585,6 @@ __device__ __forceinline__ bool estimator_score_simple(Ctx &C, int e, const PSta
     return true;
 }
 
-// Estimator::score (Estimator.cpp:298-336)
-
 // whether this particle's problem is multigroup, folded at compile time
 // where the flavour decides it
 template <int kFl>
@@ -590,15 +593,18 @@ __device__ __forceinline__ bool is_mg(const EvTables &V)
     return kFl == FL_MG ? true : (kFl == FL_CE ? false : V.G > 0);
 }
 
+// Estimator::score (Estimator.cpp:298-336).  pre / fixed as for
+// estimator_score_simple; the general path recomputes every filter.
 template <bool kGen>
-__device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, float speed, float l_in)
+__device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, float speed, float l_in, int pre,
+                                int fixed)
 {
     const EvTables &V = *C.V;
     if (!(fabsf(l_in) <= FLT_MAX)) {   // non-finite track: the loop below would never advance
         atomicCAS(C.s_status, 0, DS_NAN);
         return;
     }
-    if (estimator_score_simple(C, e, p, l_in)) return;
+    if (estimator_score_simple(C, e, p, l_in, pre, fixed)) return;
     if constexpr (!kGen) {
         atomicCAS(C.s_status, 0, DS_OVERFLOW);   // unreachable: the host picks the kGen kernel
         return;
@@ -660,14 +666,9 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
     }
     for (int wi = 0; wi < C.A->nw; ++wi) {
         unsigned long long m;
-        if (C.reg_mask) {
-            m = C.tmask;
-            C.tmask = 0ull;
+        if (C.reg_mask) {   // nw <= 2
+            m = wi == 0 ? C.tmask : C.tmask1;
             if (m == 0ull) continue;
-        } else if (C.own_rows) {
-            m = mask[wi];
-            if (m == 0ull) continue;
-            mask[wi] = 0ull;
         } else {
             if (__ldcg(mask + wi) == 0ull) continue;
             m = atomicExch(mask + wi, 0ull);
@@ -676,14 +677,9 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
             const int b = __ffsll((long long)m) - 1;
             m &= m - 1;
             const int bin = wi * 64 + b;
-            double v;
-            if (C.own_rows && !C.reg_mask) {
-                v = acc[bin];
-                acc[bin] = 0.0;
-            } else {   // the row was updated by reductions (or by other threads)
-                v = __longlong_as_double(
-                    (long long)atomicExch(reinterpret_cast<unsigned long long *>(acc + bin), 0ull));
-            }
+            // the row holds reductions: read and clear it in L2
+            const double v = __longlong_as_double(
+                (long long)atomicExch(reinterpret_cast<unsigned long long *>(acc + bin), 0ull));
             if (C.A->smem_sums) {
                 atomicAdd(C.T.ssum() + bin, v);
                 atomicAdd(C.T.ssq() + bin, v * v);
@@ -693,6 +689,8 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
             }
         }
     }
+    C.tmask = 0ull;
+    C.tmask1 = 0ull;
 }
 
 __device__ __forceinline__ void particle_dies(Ctx &C, int s, int hslot)
@@ -984,7 +982,7 @@ __device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R
     C.cnt[C_FLIGHTS]++;
     if (m >= 0 && !is_mg<kFl>(V)) C.cnt[C_NUC] += (uint32_t)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
     for (int i = V.cell_tl_off[p.cell]; i < V.cell_tl_off[p.cell + 1]; ++i)
-        estimator_score<kFl == FL_ALL>(C, V.cell_tl[i], p, t_old, speed, l);
+        estimator_score<kFl == FL_ALL>(C, V.cell_tl[i], p, t_old, speed, l, V.cell_tl_pre[i], 1);
     p.surf = -1;
     return cross ? 2 : 1;
 }
@@ -1003,7 +1001,8 @@ __device__ __forceinline__ int event_collide_begin(Ctx &C, const EvTables &V, Rn
     const int m = V.cell_mat[p.cell];
     if (m < 0) return 0;
     for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
-        estimator_score<kFl == FL_ALL>(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f);
+        estimator_score<kFl == FL_ALL>(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f,
+                                       V.cell_c_pre[i], 1);
     const float st = f.sig;
     if (is_mg<kFl>(V)) {
         const int row = m * V.G + p.g;
@@ -1088,7 +1087,7 @@ __device__ __forceinline__ bool event_cross(Ctx &C, const EvTables &V, Rng32 &R,
     if (p.wt != 0.f) {   // a vacuum boundary kills first and scores zero (general.cpp:98-111)
         const float speed = V.has_time ? speed_of(p.E) : 0.f;
         for (int i = V.surf_est_off[S]; i < V.surf_est_off[S + 1]; ++i)
-            estimator_score<kFl == FL_ALL>(C, V.surf_est[i], p, p.t, speed, 0.f);
+            estimator_score<kFl == FL_ALL>(C, V.surf_est[i], p, p.t, speed, 0.f, V.surf_est_pre[i], 0);
     }
     if (alive && p.cell != old_cell) {
         const float Iold = V.cell_imp[old_cell], Inew = V.cell_imp[p.cell];
@@ -1167,9 +1166,9 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     C.s_novf = &s_novf;
     C.s_nlive = &s_nlive;
     C.s_nhfree = &s_nhfree;
-    C.own_rows = false;
     C.reg_mask = false;
     C.tmask = 0ull;
+    C.tmask1 = 0ull;
     __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
     C.cnt.base = s_cnt + threadIdx.x;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
@@ -1420,9 +1419,9 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
     C.s_novf = nullptr;
     C.s_nlive = nullptr;
     C.s_nhfree = nullptr;
-    C.own_rows = true;
-    C.reg_mask = A.row_nb <= 64;
+    C.reg_mask = A.row_nb <= 128;
     C.tmask = 0ull;
+    C.tmask1 = 0ull;
     __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
     C.cnt.base = s_cnt + threadIdx.x;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;

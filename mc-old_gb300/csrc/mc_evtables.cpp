@@ -106,6 +106,40 @@ bool build_event_tables(const Tables &t, EvHost &h, std::string &err)
     P.add(ebo, &V.est_bin_off);
     V.has_time = 0;
     for (int k : t.filt_kind) if (k == F_TIME) V.has_time = 1;
+    // the index part of the filter an attachment fixes: the device searches
+    // FP32 grids with the id converted to float, so the same search is done
+    // here on the same values
+    auto fixed_part = [&](int e, int kind, int id) -> int {
+        int idx = 0;
+        for (int f = t.est_filt_off[e]; f < t.est_filt_off[e + 1]; ++f) {
+            if (t.filt_kind[f] != kind) continue;
+            const int i = f - t.est_filt_off[e];
+            const double *g = &t.filt_grid[t.filt_grid_off[f]];
+            const int n = t.filt_grid_len[f];
+            int left = 0, right = n - 1;
+            const float x = (float)id;
+            while (left <= right) {
+                const int mid = (left + right) >> 1;
+                if ((float)g[mid] < x) left = mid + 1;
+                else right = mid - 1;
+            }
+            const int b = right + 1;
+            if (b < 0 || b >= t.filt_size[f]) return -1;
+            idx += b * (int)t.est_factor[t.est_factor_off[e] + i + 1];
+        }
+        return idx;
+    };
+    std::vector<int> tl_pre(t.cell_tl.size()), c_pre(t.cell_c.size()), s_pre(t.surf_est.size());
+    for (int c = 0; c < t.n_cell(); ++c) {
+        for (int i = t.cell_tl_off[c]; i < t.cell_tl_off[c + 1]; ++i) tl_pre[i] = fixed_part(t.cell_tl[i], F_CELL, c);
+        for (int i = t.cell_c_off[c]; i < t.cell_c_off[c + 1]; ++i) c_pre[i] = fixed_part(t.cell_c[i], F_CELL, c);
+    }
+    for (int sf = 0; sf < t.n_surf(); ++sf)
+        for (int i = t.surf_est_off[sf]; i < t.surf_est_off[sf + 1]; ++i)
+            s_pre[i] = fixed_part(t.surf_est[i], F_SURFACE, sf);
+    P.add(tl_pre, &V.cell_tl_pre);
+    P.add(c_pre, &V.cell_c_pre);
+    P.add(s_pre, &V.surf_est_pre);
 
     // ---- continuous-energy materials ----
     V.n_mat = t.n_mat();

@@ -34,6 +34,10 @@ struct EvTables {
     const int *cell_mat, *cell_surf_off, *cell_surf, *cell_sense;
     const int *nb_off, *nb_cell;      // CSR over 2*n_surf lists: index 2*s + (sense > 0)
     const int *cell_tl_off, *cell_tl, *cell_c_off, *cell_c, *surf_est_off, *surf_est;
+    // per attachment above: the part of the flattened tally index that the
+    // estimator's cell filter (track-length, collision) or surface filter
+    // (crossing) contributes, fixed by the attachment; -1 = outside the filter
+    const int *cell_tl_pre, *cell_c_pre, *surf_est_pre;
     // estimators
     int n_est;
     long long n_bins;
