@@ -287,12 +287,21 @@ __device__ __forceinline__ float xs_at(const float *tab, const XsAt &a)
 
 enum { XT = 0, XS = 1, XC = 2 };
 
+// whether this particle's problem is multigroup, folded at compile time
+// where the flavour decides it
+template <int kFl>
+__device__ __forceinline__ bool is_mg(const EvTables &V)
+{
+    return kFl == FL_MG ? true : (kFl == FL_CE ? false : V.G > 0);
+}
+
 // macroscopic cross section of cell material at the particle's energy/group
+template <int kFl>
 __device__ __forceinline__ float macro(Ctx &C, int m, int which, const PState &p)
 {
     const EvTables &V = *C.V;
     C.cnt[C_XS]++;
-    if (V.G > 0) {
+    if (is_mg<kFl>(V)) {
         const int i = m * V.G + p.g;
         return which == XT ? __ldg(V.mg_total + i) : (which == XS ? __ldg(V.mg_scat_tot + i) : __ldg(V.mg_capture + i));
     }
@@ -524,6 +533,7 @@ __device__ __forceinline__ void tally_add(Ctx &C, int hslot, int bin, double val
     C.cnt[C_TALLY]++;
 }
 
+template <int kFl>
 __device__ float score_value(Ctx &C, int sc, const PState &p, float l)
 {
     const EvTables &V = *C.V;
@@ -531,14 +541,14 @@ __device__ float score_value(Ctx &C, int sc, const PState &p, float l)
     float k;
     switch (V.score_kernel[sc]) {
     case 0: k = p.wt * l; break;
-    case 1: k = p.wt / (m >= 0 ? macro(C, m, XT, p) : 0.f); break;
+    case 1: k = p.wt / (m >= 0 ? macro<kFl>(C, m, XT, p) : 0.f); break;
     default: k = p.wt; break;
     }
     switch (V.score_kind[sc]) {
     case 0: return k;
-    case 1: case 3: return (m >= 0 ? macro(C, m, XC, p) : 0.f) * k;
-    case 2: return (m >= 0 ? macro(C, m, XS, p) : 0.f) * k;
-    default: return (m >= 0 ? macro(C, m, XT, p) : 0.f) * k;
+    case 1: case 3: return (m >= 0 ? macro<kFl>(C, m, XC, p) : 0.f) * k;
+    case 2: return (m >= 0 ? macro<kFl>(C, m, XS, p) : 0.f) * k;
+    default: return (m >= 0 ? macro<kFl>(C, m, XT, p) : 0.f) * k;
     }
 }
 
@@ -552,6 +562,7 @@ __device__ float score_value(Ctx &C, int sc, const PState &p, float l)
 // attachment.  The table builder resolved that filter's part of the flattened
 // index once per attachment (pre; -1: the cell or surface lies outside the
 // filter, nothing is scored), and the loop skips filters of kind `fixed`.
+template <int kFl>
 __device__ __forceinline__ bool estimator_score_simple(Ctx &C, int e, const PState &p, float l_in, int pre,
                                                        int fixed)
 {
@@ -579,23 +590,16 @@ __device__ __forceinline__ bool estimator_score_simple(Ctx &C, int e, const PSta
     const int s0 = V.est_score_off[e], ns = V.est_score_off[e + 1] - s0;
     const int base = V.est_bin_off[e];
     for (int s = 0; s < ns; ++s) {
-        tally_add(C, p.hslot, base + idx1, (double)score_value(C, s0 + s, p, l_in));
+        tally_add(C, p.hslot, base + idx1, (double)score_value<kFl>(C, s0 + s, p, l_in));
         idx1 += fac[0];
     }
     return true;
 }
 
-// whether this particle's problem is multigroup, folded at compile time
-// where the flavour decides it
-template <int kFl>
-__device__ __forceinline__ bool is_mg(const EvTables &V)
-{
-    return kFl == FL_MG ? true : (kFl == FL_CE ? false : V.G > 0);
-}
 
 // Estimator::score (Estimator.cpp:298-336).  pre / fixed as for
 // estimator_score_simple; the general path recomputes every filter.
-template <bool kGen>
+template <int kFl>
 __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, float speed, float l_in, int pre,
                                 int fixed)
 {
@@ -604,9 +608,9 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
         atomicCAS(C.s_status, 0, DS_NAN);
         return;
     }
-    if (estimator_score_simple(C, e, p, l_in, pre, fixed)) return;
-    if constexpr (!kGen) {
-        atomicCAS(C.s_status, 0, DS_OVERFLOW);   // unreachable: the host picks the kGen kernel
+    if (estimator_score_simple<kFl>(C, e, p, l_in, pre, fixed)) return;
+    if constexpr (kFl != FL_ALL) {
+        atomicCAS(C.s_status, 0, DS_OVERFLOW);   // unreachable: time filters get the FL_ALL kernel
         return;
     }
     const int f0 = V.est_filt_off[e], nf = V.est_filt_off[e + 1] - f0;
@@ -634,7 +638,7 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
         int idx1 = 0;
         for (int i = 0; i < nf; ++i) idx1 += il[off[i] + idx[i]].bin * fac[i + 1];
         for (int s = 0; s < ns; ++s) {
-            tally_add(C, p.hslot, base + idx1, (double)score_value(C, s0 + s, p, l));
+            tally_add(C, p.hslot, base + idx1, (double)score_value<FL_ALL>(C, s0 + s, p, l));
             idx1 += fac[0];
         }
         for (int i = 0; i < nf; ++i) {
@@ -945,7 +949,7 @@ __device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R
     f.xa = XsAt{m, 0, 0.f};
     if (m >= 0) {
         if (is_mg<kFl>(V)) {
-            f.sig = macro(C, m, XT, p);
+            f.sig = macro<kFl>(C, m, XT, p);
         } else {
             const XsVal x = xs_eval(V, m, p.E);
             f.xa = x.at;
@@ -982,7 +986,7 @@ __device__ __forceinline__ int event_advance(Ctx &C, const EvTables &V, Rng32 &R
     C.cnt[C_FLIGHTS]++;
     if (m >= 0 && !is_mg<kFl>(V)) C.cnt[C_NUC] += (uint32_t)(V.mnuc_off[m + 1] - V.mnuc_off[m]);
     for (int i = V.cell_tl_off[p.cell]; i < V.cell_tl_off[p.cell + 1]; ++i)
-        estimator_score<kFl == FL_ALL>(C, V.cell_tl[i], p, t_old, speed, l, V.cell_tl_pre[i], 1);
+        estimator_score<kFl>(C, V.cell_tl[i], p, t_old, speed, l, V.cell_tl_pre[i], 1);
     p.surf = -1;
     return cross ? 2 : 1;
 }
@@ -1001,7 +1005,7 @@ __device__ __forceinline__ int event_collide_begin(Ctx &C, const EvTables &V, Rn
     const int m = V.cell_mat[p.cell];
     if (m < 0) return 0;
     for (int i = V.cell_c_off[p.cell]; i < V.cell_c_off[p.cell + 1]; ++i)
-        estimator_score<kFl == FL_ALL>(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f,
+        estimator_score<kFl>(C, V.cell_c[i], p, p.t, V.has_time ? speed_of(p.E) : 0.f, 0.f,
                                        V.cell_c_pre[i], 1);
     const float st = f.sig;
     if (is_mg<kFl>(V)) {
@@ -1087,7 +1091,7 @@ __device__ __forceinline__ bool event_cross(Ctx &C, const EvTables &V, Rng32 &R,
     if (p.wt != 0.f) {   // a vacuum boundary kills first and scores zero (general.cpp:98-111)
         const float speed = V.has_time ? speed_of(p.E) : 0.f;
         for (int i = V.surf_est_off[S]; i < V.surf_est_off[S + 1]; ++i)
-            estimator_score<kFl == FL_ALL>(C, V.surf_est[i], p, p.t, speed, 0.f, V.surf_est_pre[i], 0);
+            estimator_score<kFl>(C, V.surf_est[i], p, p.t, speed, 0.f, V.surf_est_pre[i], 0);
     }
     if (alive && p.cell != old_cell) {
         const float Iold = V.cell_imp[old_cell], Inew = V.cell_imp[p.cell];
