@@ -238,6 +238,8 @@ struct Ctx {
     Counters cnt;                 // spilled to A.counters before they reach 2^30
     bool reg_mask;                // own rows of at most 128 bins: the touched-bin mask is in registers
     unsigned long long tmask, tmask1;   // bins 0-63 / 64-127 the current history touched (reg_mask)
+    int cbin;                     // multigroup kernels: the history's first bin, summed in cval
+    double cval;
     int *s_status;
     int *s_novf;
     int *s_nlive;
@@ -517,8 +519,20 @@ __device__ int filter_idx_l(const EvTables &V, int f, const PState &p, float t_o
     }
 }
 
+// kFl == FL_MG: the first bin a history scores is summed in registers
+// (cbin / cval) and never goes through the row: short multigroup histories
+// often score one bin only (a leakage or reflection current).
+template <int kFl>
 __device__ __forceinline__ void tally_add(Ctx &C, int hslot, int bin, double val)
 {
+    if constexpr (kFl == FL_MG) {
+        if (C.cbin == bin || C.cbin < 0) {
+            C.cbin = bin;
+            C.cval += val;
+            C.cnt[C_TALLY]++;
+            return;
+        }
+    }
     // the value and the touched bit are reductions in L2 that the thread does
     // not wait for; rows of at most 128 bins keep the touched bits in registers
     const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
@@ -590,7 +604,7 @@ __device__ __forceinline__ bool estimator_score_simple(Ctx &C, int e, const PSta
     const int s0 = V.est_score_off[e], ns = V.est_score_off[e + 1] - s0;
     const int base = V.est_bin_off[e];
     for (int s = 0; s < ns; ++s) {
-        tally_add(C, p.hslot, base + idx1, (double)score_value<kFl>(C, s0 + s, p, l_in));
+        tally_add<kFl>(C, p.hslot, base + idx1, (double)score_value<kFl>(C, s0 + s, p, l_in));
         idx1 += fac[0];
     }
     return true;
@@ -638,7 +652,7 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
         int idx1 = 0;
         for (int i = 0; i < nf; ++i) idx1 += il[off[i] + idx[i]].bin * fac[i + 1];
         for (int s = 0; s < ns; ++s) {
-            tally_add(C, p.hslot, base + idx1, (double)score_value<FL_ALL>(C, s0 + s, p, l));
+            tally_add<FL_ALL>(C, p.hslot, base + idx1, (double)score_value<FL_ALL>(C, s0 + s, p, l));
             idx1 += fac[0];
         }
         for (int i = 0; i < nf; ++i) {
@@ -658,6 +672,7 @@ __device__ void estimator_score(Ctx &C, int e, const PState &p, float t_old, flo
 // ---------------------------------------------------------------------------
 // Folds a finished history's row into the sums (Estimator.cpp:339-346):
 // per-CTA shared sums for one problem, the problem's global sums in a batch.
+template <int kFl>
 __device__ void history_fold(Ctx &C, int hslot, int prob)
 {
     const size_t row = (size_t)blockIdx.x * C.A->tile + hslot;
@@ -667,6 +682,20 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
     if (C.A->n_prob > 0) {
         gs = C.A->psum[prob];
         gq = C.A->psq[prob];
+    }
+    if constexpr (kFl == FL_MG) {
+        if (C.cbin >= 0) {
+            const double v = C.cval;
+            if (C.A->smem_sums) {
+                atomicAdd(C.T.ssum() + C.cbin, v);
+                atomicAdd(C.T.ssq() + C.cbin, v * v);
+            } else {
+                atomicAdd(gs + C.cbin, v);
+                atomicAdd(gq + C.cbin, v * v);
+            }
+            C.cbin = -1;
+            C.cval = 0.0;
+        }
     }
     for (int wi = 0; wi < C.A->nw; ++wi) {
         unsigned long long m;
@@ -695,6 +724,8 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
     }
     C.tmask = 0ull;
     C.tmask1 = 0ull;
+    C.cbin = -1;
+    C.cval = 0.0;
 }
 
 __device__ __forceinline__ void particle_dies(Ctx &C, int s, int hslot)
@@ -703,7 +734,7 @@ __device__ __forceinline__ void particle_dies(Ctx &C, int s, int hslot)
     atomicSub(C.s_nlive, 1);
     if (atomicSub(&C.T.live()[hslot], 1) == 1) {
         __threadfence_block();
-        history_fold(C, hslot, C.T.hprob()[hslot]);
+        history_fold<FL_ALL>(C, hslot, C.T.hprob()[hslot]);
         const int k = atomicAdd(C.s_nhfree, 1);
         C.T.hfree()[k] = hslot;
     }
@@ -1173,6 +1204,8 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     C.reg_mask = false;
     C.tmask = 0ull;
     C.tmask1 = 0ull;
+    C.cbin = -1;
+    C.cval = 0.0;
     __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
     C.cnt.base = s_cnt + threadIdx.x;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
@@ -1426,6 +1459,8 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
     C.reg_mask = A.row_nb <= 128;
     C.tmask = 0ull;
     C.tmask1 = 0ull;
+    C.cbin = -1;
+    C.cval = 0.0;
     __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
     C.cnt.base = s_cnt + threadIdx.x;
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
@@ -1474,7 +1509,7 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
             if (++walks > (1u << 24)) atomicCAS(&s_status, 0, DS_TIMEOUT);
         }
         if (!have && open) {
-            history_fold(C, hslot, prob);
+            history_fold<kFl>(C, hslot, prob);
             open = false;
         }
         const bool need = !have && !exhausted;
