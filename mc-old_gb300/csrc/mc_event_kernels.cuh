@@ -552,17 +552,30 @@ __device__ float score_value(Ctx &C, int sc, const PState &p, float l)
 {
     const EvTables &V = *C.V;
     const int m = V.cell_mat[p.cell];
-    float k;
-    switch (V.score_kernel[sc]) {
-    case 0: k = p.wt * l; break;
-    case 1: k = p.wt / (m >= 0 ? macro<kFl>(C, m, XT, p) : 0.f); break;
-    default: k = p.wt; break;
+    const int kern = V.score_kernel[sc], kind = V.score_kind[sc];
+    // the cross sections this score needs come from one lookup (one copy of
+    // the lookup code per scoring site); a void cell scores zero
+    float st = 0.f, ss = 0.f, sc_ = 0.f;
+    if (m >= 0 && (kern == 1 || kind != 0)) {
+        if (is_mg<kFl>(V)) {
+            const int i = m * V.G + p.g;
+            st = __ldg(V.mg_total + i);
+            ss = __ldg(V.mg_scat_tot + i);
+            sc_ = __ldg(V.mg_capture + i);
+        } else {
+            const XsVal x = xs_eval(V, m, p.E);
+            st = x.st;
+            ss = x.ss;
+            sc_ = x.sc;
+        }
+        C.cnt[C_XS] += (kern == 1 ? 1u : 0u) + (kind != 0 ? 1u : 0u);
     }
-    switch (V.score_kind[sc]) {
+    const float k = kern == 0 ? p.wt * l : (kern == 1 ? p.wt / st : p.wt);
+    switch (kind) {
     case 0: return k;
-    case 1: case 3: return (m >= 0 ? macro<kFl>(C, m, XC, p) : 0.f) * k;
-    case 2: return (m >= 0 ? macro<kFl>(C, m, XS, p) : 0.f) * k;
-    default: return (m >= 0 ? macro<kFl>(C, m, XT, p) : 0.f) * k;
+    case 1: case 3: return sc_ * k;
+    case 2: return ss * k;
+    default: return st * k;
     }
 }
 
