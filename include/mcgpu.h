@@ -219,10 +219,19 @@ mc_status mc_forward(mc_problem *p, const double *params, uint64_t n_histories, 
 
 /* d(tally bin b)/d(param k) at the given parameters by the likelihood-ratio
  * (differential-operator) kernel, dtally[b * n_params + k], with its
- * standard error in sigma (nullable).  n_params = 2 x materials.  Density
- * derivatives follow as d/d rho_m = Sigma_s,m d/dSigma_s,m + Sigma_a,m d/dSigma_a,m. */
+ * standard error in sigma (nullable).  n_params = 2 x materials. */
 mc_status mc_backward(mc_problem *p, const double *params, uint64_t n_histories, uint64_t seed,
                       double *dtally, double *sigma);
+
+/* mc_backward plus the density derivatives in the same run:
+ * drho[b * n_materials + m] = rho_m d(tally bin b)/d rho_m, the derivative
+ * with respect to the material's density relative to its value (a density
+ * scales both cross sections of the material, so per history it is
+ * Sigma_s,m d/dSigma_s,m + Sigma_a,m d/dSigma_a,m), with its standard error
+ * in drho_sigma.  Any of the four output pointers may be NULL (not both
+ * dtally and drho). */
+mc_status mc_backward_density(mc_problem *p, const double *params, uint64_t n_histories, uint64_t seed,
+                              double *dtally, double *sigma, double *drho, double *drho_sigma);
 
 /* ---- batches: many independent problems in one persistent launch ---------
  * No counterpart in the reference, which runs one Simulator at a time.  A

@@ -64,6 +64,10 @@ struct HistoryArgs {
     // keep their score-function weights in lr_stack
     int n_params = 0;
     double *lr_stack = nullptr;   // [threads][stack_depth][n_params]
+    // derivative columns per tally bin: the n_params (Sigma_s, Sigma_a) pairs
+    // followed by one column per material for rho d/drho (density scales
+    // both cross sections of the material)
+    int n_cols = 0;
     uint32_t max_events = 1u << 22;   // events per particle before DS_TIMEOUT
 };
 

@@ -76,6 +76,7 @@ struct Ctx {
     double S[kMaxParams];
     double *lr_stack;
     int K;                 // parameters: (Sigma_s, Sigma_a) per material
+    int Kc;                // derivative columns per bin: K, then K/2 density columns
     uint32_t max_events;   // events per particle before DS_TIMEOUT
     long long nb;          // bins; the derivative rows follow the tally row
 };
@@ -419,15 +420,20 @@ __device__ void estimator_score(Ctx &C, int e, const PartD &p, double l_in)
             C.cnt[C_TALLY]++;
             if constexpr (L) {
                 // d(contribution)/d(param_k) = v S_k + direct dependence
-                double *dh = C.hist + C.nb + (size_t)(T.est_bin_off[e] + idx1) * C.K;
+                double *dh = C.hist + C.nb + (size_t)(T.est_bin_off[e] + idx1) * C.Kc;
                 double ds, da;
                 direct_terms(C, s0 + s, T.cell_mat[p.cell], p, v, ds, da);
                 const int m = T.cell_mat[p.cell];
-                for (int k = 0; k < C.K; ++k) {
-                    double d = v * C.S[k];
-                    if (m >= 0 && k == 2 * m) d += ds;
-                    if (m >= 0 && k == 2 * m + 1) d += da;
-                    dh[k] += d;
+                for (int mm = 0; mm < C.K / 2; ++mm) {
+                    double d_s = v * C.S[2 * mm], d_a = v * C.S[2 * mm + 1];
+                    if (mm == m) { d_s += ds; d_a += da; }
+                    dh[2 * mm] += d_s;
+                    dh[2 * mm + 1] += d_a;
+                    // rho d/drho = Sigma_s d/dSigma_s + Sigma_a d/dSigma_a, per history
+                    if (C.Kc > C.K) {
+                        const int i = mm * T.mg_groups;
+                        dh[C.K + mm] += T.mg_scat_tot[i] * d_s + T.mg_capture[i] * d_a;
+                    }
                 }
             }
             idx1 += (int)fac[0];
@@ -771,8 +777,9 @@ __global__ void __launch_bounds__(128) k_history_fp64(const DevTables T, const H
     const long long nb = T.n_bins;
     C.nb = nb;
     C.K = L ? A.n_params : 0;
+    C.Kc = L ? (A.n_cols > A.n_params ? A.n_cols : A.n_params) : 0;
     C.lr_stack = L ? A.lr_stack + tid * A.stack_depth * (size_t)A.n_params : nullptr;
-    const long long row = L ? nb * (1 + (long long)A.n_params) : nb;
+    const long long row = L ? nb * (1 + (long long)C.Kc) : nb;
     const bool digests = A.digest != nullptr;
     for (;;) {
         const unsigned hl = atomicAdd(A.next, 1u);

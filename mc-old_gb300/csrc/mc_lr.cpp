@@ -63,8 +63,9 @@ mc_status run_params(mc_problem *p, const double *params, uint64_t n, uint64_t s
     LrScratch &S = scratch_of(p);
     const int nm = p->t.n_mat();
     const int K = with_lr ? 2 * nm : 0;
+    const int Kc = with_lr ? 3 * nm : 0;   // (Sigma_s, Sigma_a) pairs, then rho d/drho per material
     const long long nb = std::max<long long>(d.dt.n_bins, 1);
-    const long long row = nb * (1 + K);
+    const long long row = nb * (1 + Kc);
     // one-group tables with the new values, built the way the reader builds
     // them (capture = total - scatter row sum)
     std::vector<double> tot(nm), sca(nm), stot(nm), cap(nm);
@@ -126,6 +127,7 @@ mc_status run_params(mc_problem *p, const double *params, uint64_t n, uint64_t s
         A.status = status;
         A.next = next;
         A.n_params = K;
+        A.n_cols = Kc;
         A.lr_stack = K ? static_cast<double *>(S.lrstack.ptr) : nullptr;
         if ((e = cudaMemsetAsync(next, 0, sizeof(unsigned int), d.stream)) != cudaSuccess ||
             (e = launch_history_fp64(T, A, true, grid, block, d.stream)) != cudaSuccess ||
@@ -199,19 +201,39 @@ mc_status mc_forward(mc_problem *p, const double *params, uint64_t n, uint64_t s
     return MC_OK;
 }
 
-mc_status mc_backward(mc_problem *p, const double *params, uint64_t n, uint64_t seed, double *dtally,
-                      double *sigma)
+mc_status mc_backward_density(mc_problem *p, const double *params, uint64_t n, uint64_t seed, double *dtally,
+                              double *sigma, double *drho, double *drho_sigma)
 {
     mc_status st = check_one_group(p, params);
     if (st != MC_OK) return st;
-    if (!dtally) return MC_ERR_ARG;
+    if (!dtally && !drho) return MC_ERR_ARG;
     if (n < 2) { p->err = "need at least two histories"; return MC_ERR_ARG; }
     std::vector<double> sum, sq;
     if ((st = run_params(p, params, n, seed, true, sum, sq)) != MC_OK) return st;
     const size_t nb = (size_t)p->t.n_bins();
-    const size_t K = 2 * (size_t)p->t.n_mat();
-    stats(sum, sq, std::max<size_t>(nb, 1), nb * K, (double)n, dtally, sigma);
+    const size_t nm = (size_t)p->t.n_mat();
+    const size_t K = 2 * nm, Kc = 3 * nm;
+    const size_t base = std::max<size_t>(nb, 1);
+    std::vector<double> m(Kc), s(Kc);
+    for (size_t b = 0; b < nb; ++b) {
+        stats(sum, sq, base + b * Kc, Kc, (double)n, m.data(), s.data());
+        for (size_t k = 0; k < K; ++k) {
+            if (dtally) dtally[b * K + k] = m[k];
+            if (sigma) sigma[b * K + k] = s[k];
+        }
+        for (size_t k = 0; k < nm; ++k) {
+            if (drho) drho[b * nm + k] = m[K + k];
+            if (drho_sigma) drho_sigma[b * nm + k] = s[K + k];
+        }
+    }
     return MC_OK;
+}
+
+mc_status mc_backward(mc_problem *p, const double *params, uint64_t n, uint64_t seed, double *dtally,
+                      double *sigma)
+{
+    if (!dtally) return MC_ERR_ARG;
+    return mc_backward_density(p, params, n, seed, dtally, sigma, nullptr, nullptr);
 }
 
 }  // extern "C"

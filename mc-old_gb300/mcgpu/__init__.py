@@ -96,6 +96,7 @@ def lib() -> ctypes.CDLL:
         L.mc_lr_params.argtypes = [P, P, u32]
         L.mc_forward.argtypes = [P, P, u64, u64, P, P]
         L.mc_backward.argtypes = [P, P, u64, u64, P, P]
+        L.mc_backward_density.argtypes = [P, P, u64, u64, P, P, P, P]
         L.mc_batch_create.argtypes = [ctypes.POINTER(P), u32, ctypes.POINTER(u64), ctypes.POINTER(P)]
         L.mc_batch_run.argtypes = [P, u64, ctypes.POINTER(Tune)]
         L.mc_batch_counters.argtypes = [P, ctypes.POINTER(Counters)]
@@ -111,7 +112,7 @@ def lib() -> ctypes.CDLL:
                   "mc_problem_table_bytes", "mc_run", "mc_reset_tallies",
                   "mc_tally_count", "mc_tally_size", "mc_estimator_name", "mc_tally_read",
                   "mc_counters_read", "mc_digests_read", "mc_nsample", "mc_histories_run",
-                  "mc_report", "mc_state_save", "mc_state_load", "mc_autotune", "mc_lr_params", "mc_forward", "mc_backward", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
+                  "mc_report", "mc_state_save", "mc_state_load", "mc_autotune", "mc_lr_params", "mc_forward", "mc_backward", "mc_backward_density", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
                   "mc_batch_autotune", "mc_batch_free"):
             getattr(L, f).restype = st
         _lib = L
@@ -262,6 +263,22 @@ class Problem:
         s = np.zeros(max(nb * K, 1))
         self._check(lib().mc_backward(self._h, p.ctypes.data, n, seed, d.ctypes.data, s.ctypes.data))
         return d[: nb * K].reshape(nb, K), s[: nb * K].reshape(nb, K)
+
+    def backward_density(self, params, n: int, seed: int = DEFAULT_SEED):
+        """(d tally / d params, sigma, rho d tally / d rho, sigma), shaped
+        [bins, params] and [bins, materials], from one run."""
+        p = np.ascontiguousarray(params, np.float64)
+        nb = int(sum(self.sizes))
+        K = p.size
+        M = K // 2
+        d = np.zeros(max(nb * K, 1))
+        s = np.zeros(max(nb * K, 1))
+        r = np.zeros(max(nb * M, 1))
+        rs = np.zeros(max(nb * M, 1))
+        self._check(lib().mc_backward_density(self._h, p.ctypes.data, n, seed, d.ctypes.data, s.ctypes.data,
+                                              r.ctypes.data, rs.ctypes.data))
+        return (d[: nb * K].reshape(nb, K), s[: nb * K].reshape(nb, K),
+                r[: nb * M].reshape(nb, M), rs[: nb * M].reshape(nb, M))
 
     def autotune(self, sample: int = 200000, seed: int = DEFAULT_SEED) -> dict:
         """Pick and keep the event engine's fastest launch shape."""

@@ -113,3 +113,42 @@ def test_backward_matches_deterministic_derivative(mc):
             td = solve_slab([w] * R, dn_s + dn_a, dn_s, n_mu=48, dx_max=0.0125)["transmission"]
             exact = (tu - td) / (2 * h)
             assert abs(g[0, k] - exact) <= 4 * gs[0, k] + 1e-3 * abs(exact), (r, which, g[0, k], exact, gs[0, k])
+
+
+def test_density_derivatives(mc):
+    """rho d(T)/d(rho) per region from the same backward run: equal to
+    Sigma_s dT/dSigma_s + Sigma_a dT/dSigma_a, with its own per-history
+    standard error, and equal to the S_N derivative for a density scaling
+    of one region of the homogeneous slab."""
+    from analytic import solve_slab
+    R, w = 16, 0.25
+    tot, c = np.full(R, 1.0), np.full(R, 0.5)
+    with tempfile.TemporaryDirectory() as d:
+        import mcgpu.workloads as W
+        W.mg_layered_slab(d, samples=1000, n_regions=R, tot=tot, c=c)
+        import re
+        txt = open(d + "/input.xml").read()
+        txt = re.sub(r'<plane_x name="p(\d+)" x="[^"]*"/>',
+                     lambda m_: f'<plane_x name="p{m_.group(1)}" x="{int(m_.group(1)) * w!r}"/>', txt)
+        open(d + "/input.xml", "w").write(txt)
+        p = mc.Problem(d)
+        par = p.lr_params()
+        g, gs, r, rs = p.backward_density(par, 2_000_000, seed=5)
+        g2, gs2 = p.backward(par, 2_000_000, seed=5)
+        p.close()
+    assert np.array_equal(g, g2) and np.array_equal(gs, gs2)
+    ss, sa = par[0::2], par[1::2]
+    combo = ss * g[0, 0::2] + sa * g[0, 1::2]
+    assert np.allclose(r[0], combo, rtol=1e-9, atol=1e-15)
+    assert np.all(rs[0] > 0)
+    for reg in (0, 7, 15):
+        h = 1e-4
+        up_s, up_a, dn_s, dn_a = ss.copy(), sa.copy(), ss.copy(), sa.copy()
+        up_s[reg] *= 1 + h
+        up_a[reg] *= 1 + h
+        dn_s[reg] *= 1 - h
+        dn_a[reg] *= 1 - h
+        tu = solve_slab([w] * R, up_s + up_a, up_s, n_mu=48, dx_max=0.0125)["transmission"]
+        td = solve_slab([w] * R, dn_s + dn_a, dn_s, n_mu=48, dx_max=0.0125)["transmission"]
+        exact = (tu - td) / (2 * h)
+        assert abs(r[0, reg] - exact) <= 4 * rs[0, reg] + 1e-3 * abs(exact), (reg, r[0, reg], exact, rs[0, reg])
