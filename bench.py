@@ -335,7 +335,9 @@ def gpu_arm(a):
         "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {"event": "f32 tracking / f64 tallies", "plain": "f64", "replay": "f64"}[a.mode],
+        "dtype": {"event": "f32", "plain": "f64", "replay": "f64"}[a.mode],
+        "dtype_detail": {"event": "f32 tracking, f64 tally accumulation", "plain": "f64",
+                         "replay": "f64, the reference's operation order"}[a.mode],
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "histories_per_step": H, "mode": a.mode,
                    "launch_shape": _shape(tuned),
@@ -402,7 +404,8 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
     total = sum(hist)
     line = {"metric": METRIC, "value": total / T, "unit": "histories/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": T * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 tracking / f64 tallies", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32", "dtype_detail": "f32 tracking, f64 tally accumulation",
+            "data": "synthetic",
             "config": {"workload": f"batch_shields: {len(hist)} MG slab/sphere shields, {total} histories, "
                                    "one persistent launch from a CUDA graph",
                        "launch_shape": _shape(tuned),
