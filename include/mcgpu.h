@@ -54,7 +54,10 @@ typedef enum {
      * tile of particles per CTA (structure of arrays in shared memory,
      * ballot/prefix-sum compacted collision and crossing queues), or one
      * particle per thread in registers; both sample free-gas targets for a
-     * whole warp at once.  mc_tune.kernel or mc_autotune picks one. */
+     * whole warp at once.  mc_tune.kernel or mc_autotune picks one; the
+     * default is the per-thread kernel.  A problem with the particle comb
+     * (population_control.cpp:55-84) runs on the per-thread kernel, which
+     * keeps each history's bank on its thread's stack. */
     MC_MIXED_EVENT = 2
 } mc_mode;
 
@@ -64,7 +67,8 @@ typedef struct {
     uint32_t block;          /* threads per block (0 = default) */
     uint32_t grid_blocks;    /* blocks, 0 = fill the GPU */
     uint32_t stack_depth;    /* split-particle stack per thread: FP64 modes and the
-                                per-thread event kernel (0 = 32) */
+                                per-thread event kernel (0 = 32, or teeth + 32
+                                with the particle comb) */
     uint32_t chunk;          /* FP64 modes: histories per fold chunk (0 = auto) */
     uint32_t bank_capacity;  /* event mode: particles per CTA tile (0 = tuned / 512) */
     uint32_t record_digests; /* FP64 modes: keep per-history event digests */
@@ -73,7 +77,8 @@ typedef struct {
                                 (256 threads), 4, 6, 7 or 8 for the per-thread
                                 kernel (128 threads); 0 = tuned / 4 / 8 */
     uint32_t kernel;         /* event mode: 1 = particle tile with event queues,
-                                2 = one particle per thread, 0 = tuned / 1 */
+                                2 = one particle per thread, 0 = tuned / 2;
+                                the tile kernel refuses the particle comb */
     uint32_t max_events;     /* events one particle may take before the run stops
                                 with MC_ERR_TIMEOUT (0 = 2^22); a small cap
                                 exercises that path on purpose */

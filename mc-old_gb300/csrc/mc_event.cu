@@ -104,12 +104,6 @@ EvKernel pick_kernel(int minb, bool batch, int kernel, int flavor)
 
 bool event_tables_ready(const Tables &t, DeviceProblem &d, std::string &err)
 {
-    if (t.comb_teeth > 0) {
-        // the comb acts on one history's bank after each walk; the event
-        // engine runs a history's particles side by side and has no such bank
-        err = "the particle comb needs the history-ordered FP64 modes (MC_FP64_REPLAY or MC_FP64_PLAIN)";
-        return false;
-    }
     if (d.ev_state) return true;
     EventState *S = new EventState();
     if (!build_event_tables(t, S->host, err)) { delete S; return false; }
@@ -139,12 +133,21 @@ struct EvLaunch {
 };
 
 static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune, const mc_tune &tuned,
-                                    long long nb_smem, bool batch, int flavor, EvLaunch &L,
+                                    long long nb_smem, bool batch, int flavor, int comb_teeth, EvLaunch &L,
                                     std::string &err)
 {
     L.flavor = flavor;
-    L.kernel = (tune && tune->kernel) ? (int)tune->kernel : (tuned.kernel ? (int)tuned.kernel : 1);
+    L.kernel = (tune && tune->kernel) ? (int)tune->kernel : (tuned.kernel ? (int)tuned.kernel : 2);
     if (L.kernel < 1 || L.kernel > 2) { err = "kernel must be 1 (tile) or 2 (per thread)"; return MC_ERR_ARG; }
+    if (comb_teeth > 0 && L.kernel != 2) {
+        // the comb acts on one history's bank after each walk; the tile
+        // kernel runs a history's particles side by side and has no such bank
+        if (tune && tune->kernel) {
+            err = "the particle comb needs a per-history bank: the per-thread kernel (kernel 2) or the FP64 modes";
+            return MC_ERR_ARG;
+        }
+        L.kernel = 2;   // a tuned tile shape does not apply to a combed problem
+    }
     const int block = L.kernel == 2 ? kTrackBlock : 256;
     L.block = (tune && tune->block) ? (int)tune->block : block;
     if (L.block != block) {
@@ -163,8 +166,15 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
     }
     if (L.kernel == 2) {
         L.tile = kTrackBlock;                  // one history row per thread
-        const int depth = (tune && tune->stack_depth) ? (int)tune->stack_depth : kTrackDepth;
-        if (depth < 1 || depth > 4096) { err = "stack_depth must be 1..4096"; return MC_ERR_ARG; }
+        // a combed stack holds `teeth` particles plus the split copies of one walk
+        const int depth = (tune && tune->stack_depth) ? (int)tune->stack_depth
+                                                      : std::max(kTrackDepth, comb_teeth + kTrackDepth);
+        if (depth < 1 || depth > 4096) {
+            err = comb_teeth > 0 && !(tune && tune->stack_depth)
+                      ? "the per-thread kernel keeps at most 4064 comb teeth"
+                      : "stack_depth must be 1..4096";
+            return MC_ERR_ARG;
+        }
         L.ovf_cap = kTrackBlock * depth;
         L.smem = sizeof(double) * 2 * (size_t)nb_smem + 64;
     } else {
@@ -237,8 +247,9 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     const long long nb = std::max<long long>(V.n_bins, 1);
     const bool smem_sums = nb <= 4096;
     EvLaunch L;
-    const int flavor = V.has_time ? FL_ALL : (V.G > 0 ? FL_MG : FL_CE);
-    mc_status st = event_launch_shape(d, tune, d.tuned, smem_sums ? nb : 0, false, flavor, L, err);
+    const int comb = t.comb_teeth > 0 ? t.comb_teeth : 0;
+    const int flavor = (V.has_time || comb) ? FL_ALL : (V.G > 0 ? FL_MG : FL_CE);
+    mc_status st = event_launch_shape(d, tune, d.tuned, smem_sums ? nb : 0, false, flavor, comb, L, err);
     if (st != MC_OK) return st;
     if ((st = event_scratch(S, d.stream, L.grid, L.tile, L.ovf_cap, nb, err)) != MC_OK) return st;
     char *misc = static_cast<char *>(S.misc.ptr);
@@ -261,6 +272,8 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     A.sq = d.d_sq;
     A.tile = L.tile;
     A.smem_sums = smem_sums ? 1 : 0;
+    A.comb_bank_max = comb ? t.comb_bank_max : 0;
+    A.comb_teeth = comb;
     A.n_prob = 0;
     cudaEventRecord(d.ev[0], d.stream);
     pick_kernel(L.minb, false, L.kernel, L.flavor)<<<L.grid, L.block, L.smem, d.stream>>>(V, A);
@@ -344,6 +357,12 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
     std::vector<unsigned long long> prefix(n + 1, 0);
     std::vector<double *> psum(n), psq(n);
     for (uint32_t i = 0; i < n; ++i) {
+        if (tabs[i]->comb_teeth > 0) {
+            // a lane of the batch kernel keeps no comb state per problem
+            batch_state_free(b);
+            err = "problem " + std::to_string(i) + ": batches do not run the particle comb (mc_run does)";
+            return MC_ERR_INPUT;
+        }
         if (!event_tables_ready(*tabs[i], *probs[i], err)) { batch_state_free(b); err = "problem " + std::to_string(i) + ": " + err; return MC_ERR_INPUT; }
         views[i] = probs[i]->ev_state->dv;
         prefix[i + 1] = prefix[i] + hist[i];
@@ -400,7 +419,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     DeviceProblem shape_dev;
     shape_dev.sms = device_sms;
     EvLaunch L;
-    mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, b->flavor, L, err);
+    mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, b->flavor, 0, L, err);
     if (st != MC_OK) return st;
     if ((st = event_scratch(b->scratch, b->stream, L.grid, L.tile, L.ovf_cap, b->row_nb, err)) != MC_OK) return st;
     L.max_events = (tune && tune->max_events) ? tune->max_events : kMaxEvents;

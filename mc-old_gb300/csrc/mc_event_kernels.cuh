@@ -38,6 +38,7 @@ struct EvArgs {
     int *status;
     int tile;
     int smem_sums;                // per-CTA sums live in shared memory
+    int comb_bank_max, comb_teeth;  // particle comb on the per-thread stack (0 teeth: off)
     // batch of problems (kBatch): history index space = concatenation of
     // every problem's histories
     const EvTables *tabs;         // [n_prob]
@@ -59,9 +60,10 @@ enum TileArray {
 // Kernel flavours: what code a per-thread kernel carries.  A kernel built
 // for one kind of problem leaves out the rest, which would otherwise cost the
 // hot loop registers and instruction-cache room.
-//   FL_ALL  everything: continuous-energy and multigroup physics, and the
+//   FL_ALL  everything: continuous-energy and multigroup physics, the
 //           general scoring path for time filters (one flight may cover
-//           several bins, through a pair list in local memory);
+//           several bins, through a pair list in local memory) and the
+//           particle comb;
 //   FL_CE   continuous energy, no time filter;
 //   FL_MG   multigroup, no time filter.
 enum Flavor { FL_ALL = 0, FL_CE = 1, FL_MG = 2 };
@@ -1445,6 +1447,43 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     }
 }
 
+// population_control.cpp:55-84 on a thread's own stack, after every walk
+// (handler.cpp:27), keyed as the FP64 engines' comb: the first tooth is one
+// uniform from the stream of the particle that just walked, at event
+// kCombEvent; tooth j is filled in place from entry i >= j (a particle passes
+// at most one tooth, the reference's `if`); teeth left over hold the bottom
+// entry with its own weight (bank_tmp(teeth, Pbank[0])); the combed copies
+// are renamed child_id(walker, kCombEvent, j + 1).  The weights are summed in
+// FP64.  Returns the new stack height (teeth).  Out of line: it runs once per
+// combed walk, and its loops stay out of the event loop's instruction stream.
+constexpr uint32_t kCombEvent = 0xFFFFFFFFu;
+
+__device__ __noinline__ int comb_stack(OvfP *stk, int sp, int teeth, uint64_t seed, uint64_t hist,
+                                       uint32_t walker)
+{
+    double W = 0.0;
+    for (int i = 0; i < sp; ++i) W += (double)stk[i].wt;
+    const double w_avg = W / (double)teeth;
+    Rng32 R;
+    R.init(seed, hist, walker, kCombEvent, 0u);
+    double tooth = (double)R.next() * w_avg;
+    const OvfP first = stk[0];
+    double sum = 0.0;
+    int j = 0;
+    for (int i = 0; i < sp; ++i) {
+        sum += (double)stk[i].wt;
+        if (sum > tooth && j < teeth) {   // j < teeth: rounding cannot add a tooth
+            OvfP q = stk[i];
+            q.wt = (float)w_avg;
+            stk[j++] = q;
+            tooth += w_avg;
+        }
+    }
+    for (int k = j; k < teeth; ++k) stk[k] = first;
+    for (int k = 0; k < teeth; ++k) stk[k].id = child_id(walker, kCombEvent, (uint32_t)(k + 1));
+    return teeth;
+}
+
 // The per-thread loop: each thread carries one particle through event after
 // event in registers (advance, then collision or crossing, with the same
 // event functions and Philox keying as k_event), keeps its history's split
@@ -1510,6 +1549,11 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
         return true;
     };
     for (uint32_t it = 1;; ++it) {
+        if constexpr (kFl == FL_ALL && !kBatch) {
+            // a walk has just ended whenever the stack is non-empty here
+            if (!have && A.comb_teeth > 0 && sp >= A.comb_bank_max)
+                sp = comb_stack(stk, sp, A.comb_teeth, A.seed, hist, p.id);
+        }
         // the next particle: the history's own split copies first (LIFO, as
         // the reference's bank), then a new history
         if (!have && sp > 0) {

@@ -1,11 +1,13 @@
 """Particle comb (population_control.cpp:55-84, setup.cpp:57-67) on the GPU.
 
-The comb runs in the history-ordered FP64 modes.  Replay reproduces the
+The comb runs in the history-ordered FP64 modes and in the per-thread FP32
+kernel, each of which keeps one history's bank.  Replay reproduces the
 oracle's event digests and tally sums bit for bit for several (bank_max,
 teeth) pairs.  The oracle's comb is pinned to the compiled reference's own
-particle_comb by the comb_slab golden fixture.  Plain FP64 agrees with replay
-statistically.  The event engine and batches refuse a combed problem with a
-status, because they keep no per-history bank."""
+particle_comb by the comb_slab golden fixture.  Plain FP64 and the mixed
+per-thread kernel agree with replay statistically.  The tile kernel and
+batches refuse a combed problem with a status, because they keep no
+per-history bank."""
 import tempfile
 
 import numpy as np
@@ -58,15 +60,54 @@ def test_comb_plain_agrees_with_replay(mc):
     assert both.sum() > 50 and np.mean(z <= 3.0) >= 0.97, np.sort(z)[-5:]
 
 
+@pytest.mark.parametrize("bank_max,teeth", [(3, 2), (1, 1), (6, 4)])
+def test_comb_mixed_agrees_with_replay(mc, bank_max, teeth):
+    """The per-thread kernel's comb (FP32 tracking, FP64 weight sums) against
+    FP64 replay of the same problem: every resolved bin within 3 sigma in at
+    least 97 % of the bins, and the population per history equal in
+    expectation (particles / histories within 5 sigma of replay's)."""
+    with tempfile.TemporaryDirectory() as d:
+        cases.comb_slab(d, samples=40000, bank_max=bank_max, teeth=teeth)
+        p = mc.Problem(d, d + "/xs_library")
+        cr = p.run(mode="replay")
+        m1, s1, _, _ = p.all_tallies()
+        p.reset()
+        ce = p.run(mode="event", seed=mc.DEFAULT_SEED + 7, kernel=2)
+        m2, s2, _, _ = p.all_tallies()
+        p.close()
+    both = (s1 > 0) & (s2 > 0)
+    z = np.abs(m1 - m2)[both] / np.sqrt(s1[both] ** 2 + s2[both] ** 2)
+    assert both.sum() > 50 and np.mean(z <= 3.0) >= 0.97, np.sort(z)[-5:]
+    assert ce["histories"] == cr["histories"]
+    # particles per history: a rough check that the comb fires as often
+    a, b = cr["particles"] / cr["histories"], ce["particles"] / ce["histories"]
+    assert abs(a - b) <= 0.05 * a, (a, b)
+
+
+def test_comb_mixed_default_shape_and_tuned_tile_shape(mc):
+    """Without a tune the mixed mode runs the per-thread kernel; a problem
+    autotuned with the comb picks a per-thread shape."""
+    with tempfile.TemporaryDirectory() as d:
+        cases.comb_slab(d, samples=2000, bank_max=3, teeth=2)
+        p = mc.Problem(d, d + "/xs_library")
+        c = p.run(mode="event")
+        assert c["histories"] == 2000
+        t = p.autotune(sample=4000)
+        assert t["kernel"] == 2
+        p.reset()
+        p.run(mode="event")
+        p.close()
+
+
 def test_comb_refused_where_no_history_bank_exists(mc):
     with tempfile.TemporaryDirectory() as d:
         cases.comb_slab(d, samples=100)
         p = mc.Problem(d, d + "/xs_library")
         with pytest.raises(mc.McError) as e:
-            p.run(mode="event")
-        assert e.value.status == 1 and "comb" in str(e.value)
+            p.run(mode="event", kernel=1)
+        assert e.value.status == 8 and "comb" in str(e.value)    # MC_ERR_ARG
         with pytest.raises(mc.McError) as e:
             mc.Batch([p], [100])
-        assert e.value.status == 1
+        assert e.value.status == 1 and "comb" in str(e.value)
         p.run(n=50, mode="replay")     # the handle stays usable
         p.close()

@@ -118,7 +118,7 @@ def test_event_tiles_and_grids(mc):
         cases.write_case("slab_features", d)
         ref = _run(mc, d, 20000, "event")
         for tile, grid in ((256, 7), (1024, 0), (512, 1)):
-            m, s, c = _run(mc, d, 20000, "event", bank_capacity=tile, grid_blocks=grid)
+            m, s, c = _run(mc, d, 20000, "event", kernel=1, bank_capacity=tile, grid_blocks=grid)
             assert c["histories"] == 20000
             assert_agree(m, s, ref[0], ref[1], f"tile {tile} grid {grid}")
         for minb, grid in ((4, 0), (6, 5), (8, 1)):
