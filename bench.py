@@ -27,6 +27,8 @@ roofline   the transport kernels against HBM: algorithmic bytes per run =
            nuclide; tally: one FP64 read-modify-write), from the device
            counters, over the transport kernels' CUDA-event time; peak =
            MEASURED_PEAKS.json hbm_gbs; traffic from the committed ncu summary.
+roofline_l2  the same algorithmic bytes against an L2 read bandwidth measured
+           in the run (the tables are L2-resident).
 cpu_baseline  the CPU oracle (a C restatement of the reference's history loop)
            on the host cores, on a bounded sample of the same workload.
 
@@ -128,6 +130,32 @@ def _measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
+def _l2_read_gbs(torch):
+    """L2 read bandwidth, measured here: one reduction kernel sums each of 64
+    rows that all alias the same 32 MiB FP32 buffer (a stride-0 view; the
+    buffer stays resident in the 129 MB L2), 2 GiB of reads per launch, over
+    the CUDA-event time, best of 5 after warm-up.  MEASURED_PEAKS.json holds
+    no L2 figure; the cross-section tables of these workloads live in L2, so
+    the algorithmic bytes are also set against this."""
+    n, reps = 8 << 20, 64
+    a = torch.ones(n, dtype=torch.float32, device="cuda")
+    v = a.expand(reps, n)
+    out = torch.empty(reps, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        torch.sum(v, dim=1, out=out)
+    best = 0.0
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.sum(v, dim=1, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 4.0 * n * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    del a, v, out
+    return best
+
+
 def _shape(tuned):
     """The autotuned launch shape: kernel 1 = particle tile with event queues
     (tile particles per CTA), kernel 2 = one particle per thread."""
@@ -142,7 +170,9 @@ def _traffic_key(mode, tuned):
     """Key of the dominant kernel in profiles/traffic.json."""
     if mode != "event":
         return mode
-    return "event:k_track" if tuned and tuned.get("kernel") == 2 else "event:k_event"
+    if tuned and tuned.get("kernel") == 2:
+        return "event:k_track:%d" % tuned["blocks_per_sm"]   # by CTAs per SM
+    return "event:k_event"
 
 
 def _ncu_traffic():
@@ -322,6 +352,7 @@ def gpu_arm(a):
     achieved = alg_bytes / (transport_ms * 1e-3) / 1e9 if transport_ms > 0 else 0.0
     traffic = _ncu_traffic()
     peak = float(peaks.get("hbm_gbs", 6800.0))
+    l2_peak = _l2_read_gbs(torch)
     cpu = None
     if a.cpu_baseline:
         with tempfile.TemporaryDirectory() as tmp:
@@ -351,6 +382,9 @@ def gpu_arm(a):
                      "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs",
                      "algorithmic_bytes_per_step": alg_bytes / a.steps,
                      "kernel_ms_per_step": transport_ms / a.steps},
+        "roofline_l2": {"bound": "l2", "achieved": achieved, "peak": l2_peak, "unit": "GB/s",
+                        "frac": achieved / l2_peak if l2_peak else None,
+                        "peak_source": "measured in this run: one reduction kernel reading a 32 MiB L2-resident buffer 64 times"},
         "counters_per_step": {k: v / a.steps for k, v in cnt_sum.items()},
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": h2d,
