@@ -845,9 +845,10 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int n)
 }
 
 // The rejection loop for every pending lane of the warp at once; all 32
-// lanes must call it.  Each round every lane evaluates one candidate: lane L
-// works on pending particle (L mod np) at offset (L div np) past the
-// candidates that particle has already tried.  A particle takes its first
+// lanes must call it.  After the first round (each particle's own first
+// candidate), each round every lane evaluates one candidate: lane L works on
+// pending particle (L mod np) at offset (L div np) past the candidates that
+// particle has already tried.  A particle takes its first
 // accepted candidate in candidate order, which is the one the sequential loop
 // accepts; a warp needs about two rounds where the sequential loop needs the
 // longest rejection chain among its lanes.
@@ -860,21 +861,41 @@ __device__ __forceinline__ bool warp_free_gas(Ctx &C, bool pend, const Rng32 &R,
         const unsigned pm = __ballot_sync(0xffffffffu, pend);
         if (pm == 0u) return true;
         if (round >= kFgMaxCandidates) return !pend;
+        // round 0: each pending particle tries its own first candidate in its
+        // own lane; later rounds share the lanes among the pending particles
         const int np = __popc(pm);
-        const int which = lane % np, off = lane / np;
-        const int src = nth_set_bit(pm, which);
-        const float s_speed = __shfl_sync(0xffffffffu, g.speed, src);
-        const float s_beta = __shfl_sync(0xffffffffu, g.beta, src);
-        const float s_pg2 = __shfl_sync(0xffffffffu, g.p_g2, src);
-        const uint32_t s_k0 = __shfl_sync(0xffffffffu, R.k0, src);
-        const uint32_t s_k1 = __shfl_sync(0xffffffffu, R.k1, src);
-        const uint32_t s_hlo = __shfl_sync(0xffffffffu, R.hlo, src);
-        const uint32_t s_id = __shfl_sync(0xffffffffu, R.id, src);
-        const uint32_t s_ev = __shfl_sync(0xffffffffu, R.ev, src);
-        const uint32_t s_tried = __shfl_sync(0xffffffffu, tried, src);
+        int which = 0, off = 0, src = lane;
+        float s_speed = g.speed, s_beta = g.beta, s_pg2 = g.p_g2;
+        uint32_t s_k0 = R.k0, s_k1 = R.k1, s_hlo = R.hlo, s_id = R.id, s_ev = R.ev, s_tried = 0u;
+        if (round > 0) {
+            which = lane % np;
+            off = lane / np;
+            src = nth_set_bit(pm, which);
+            s_speed = __shfl_sync(0xffffffffu, g.speed, src);
+            s_beta = __shfl_sync(0xffffffffu, g.beta, src);
+            s_pg2 = __shfl_sync(0xffffffffu, g.p_g2, src);
+            s_k0 = __shfl_sync(0xffffffffu, R.k0, src);
+            s_k1 = __shfl_sync(0xffffffffu, R.k1, src);
+            s_hlo = __shfl_sync(0xffffffffu, R.hlo, src);
+            s_id = __shfl_sync(0xffffffffu, R.id, src);
+            s_ev = __shfl_sync(0xffffffffu, R.ev, src);
+            s_tried = __shfl_sync(0xffffffffu, tried, src);
+        }
         float Vc, muc;
         const bool hit = fg_candidate(s_speed, s_beta, s_pg2, s_k0, s_k1, s_hlo, s_id, s_ev,
                                       s_tried + (uint32_t)off, Vc, muc);
+        if (round == 0) {
+            if (pend) {
+                tried = 1u;
+                if (hit) {
+                    C.cnt[C_FREEGAS] += 1u;
+                    V = Vc;
+                    mu = muc;
+                    pend = false;
+                }
+            }
+            continue;
+        }
         const unsigned sm = __ballot_sync(0xffffffffu, hit);
         int first = -1, r = 0;
         if (pend) {
