@@ -832,6 +832,14 @@ __device__ __forceinline__ bool fg_candidate(float speed, float beta, float p_g2
 
 constexpr uint32_t kFgMaxCandidates = 1u << 16;
 
+// a / b for 0 <= a <= 64 and 1 <= b <= 32, exactly: (a + 1/2) / b lies at
+// least 1/64 from an integer, far more than the rounding of one reciprocal
+// and one product (checked for every pair by the test suite's restatement)
+__device__ __forceinline__ int div_small(int a, int b)
+{
+    return (int)__fmul_rn(__fadd_rn((float)a, 0.5f), __frcp_rn((float)b));
+}
+
 // position of the n-th (0-based) set bit of m; n < popc(m)
 __device__ __forceinline__ int nth_set_bit(unsigned m, int n)
 {
@@ -868,8 +876,8 @@ __device__ __forceinline__ bool warp_free_gas(Ctx &C, bool pend, const Rng32 &R,
         float s_speed = g.speed, s_beta = g.beta, s_pg2 = g.p_g2;
         uint32_t s_k0 = R.k0, s_k1 = R.k1, s_hlo = R.hlo, s_id = R.id, s_ev = R.ev, s_tried = 0u;
         if (round > 0) {
-            which = lane % np;
-            off = lane / np;
+            off = div_small(lane, np);
+            which = lane - off * np;
             src = nth_set_bit(pm, which);
             s_speed = __shfl_sync(0xffffffffu, g.speed, src);
             s_beta = __shfl_sync(0xffffffffu, g.beta, src);
@@ -908,13 +916,13 @@ __device__ __forceinline__ bool warp_free_gas(Ctx &C, bool pend, const Rng32 &R,
         const float ms = __shfl_sync(0xffffffffu, muc, sel);
         if (pend) {
             if (first >= 0) {
-                tried += (uint32_t)(first / np) + 1u;
+                tried += (uint32_t)div_small(first, np) + 1u;
                 C.cnt[C_FREEGAS] += tried;
                 V = Vs;
                 mu = ms;
                 pend = false;
             } else {
-                tried += (uint32_t)((32 - r + np - 1) / np);
+                tried += (uint32_t)div_small(32 - r + np - 1, np);
             }
         }
     }
