@@ -869,8 +869,9 @@ __device__ __forceinline__ bool warp_free_gas(Ctx &C, bool pend, const Rng32 &R,
         const unsigned pm = __ballot_sync(0xffffffffu, pend);
         if (pm == 0u) return true;
         if (round >= kFgMaxCandidates) return !pend;
-        // round 0: each pending particle tries its own first candidate in its
-        // own lane; later rounds share the lanes among the pending particles
+        // the first round: each pending particle tries its own first
+        // candidate in its own lane; later rounds share the lanes among the
+        // pending particles
         const int np = __popc(pm);
         int which = 0, off = 0, src = lane;
         float s_speed = g.speed, s_beta = g.beta, s_pg2 = g.p_g2;

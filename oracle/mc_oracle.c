@@ -1,7 +1,7 @@
 /*
  * mc_oracle.c -- CPU oracle for the fixed-source particle-history path.
  *
- * TEST INFRASTRUCTURE.  This file is the checker: it restates, in plain C, the
+ * TEST INFRASTRUCTURE.  This file is the oracle: it restates, in plain C, the
  * reference's algorithm for this path so that the CUDA library can be
  * compared with it.  Only tests/, __graft_entry__.smoke() and the CPU-baseline
  * leg of bench.py may load it.  Each function names the reference lines it

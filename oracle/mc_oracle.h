@@ -1,7 +1,7 @@
 /*
  * mc_oracle.h -- CPU oracle for the fixed-source particle-history path.
  *
- * TEST INFRASTRUCTURE.  This is the checker, not the product: only tests/,
+ * TEST INFRASTRUCTURE.  This is the oracle, not the product: only tests/,
  * __graft_entry__.smoke() and the CPU-baseline leg of bench.py load it.  It is
  * a plain-C restatement of the reference's history loop (MC-old,
  * src/simulator/handler.cpp:11-48, src/simulator/general.cpp:13-211) and of

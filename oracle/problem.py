@@ -1,12 +1,12 @@
 """CPU oracle front end: input.xml -> flat arrays -> mc_oracle.c.
 
-TEST INFRASTRUCTURE.  This module is the checker's own reader of the
+TEST INFRASTRUCTURE.  This module is the oracle's own reader of the
 reference's XML schema (MC-old src/simulator/setup.cpp:30-1066).  It is
 independent of the product's C++ reader on purpose: the two are compared on
 the same inputs.  Only tests/, __graft_entry__.smoke() and the CPU-baseline
 leg of bench.py may import it.
 
-Schema extensions beyond the reference (documented in the design doc):
+Schema extensions beyond the reference:
   <population_control><weight_roulette wr=".." ws=".."/>   (simulator.h:90-91)
   <multigroup groups="G"/> plus <material><multigroup total=".." scatter=".."/>
   <isotropic_hemisphere name=".." datatype="point"/>  (cosine to +x ~ U(0,1))
