@@ -110,14 +110,16 @@ typedef struct {
  * xs_dir NULL means "./xs_library" as in the reference (setup.cpp:326). */
 mc_status mc_problem_load_xml(const char *io_dir, const char *xs_dir, mc_problem **out);
 
-/* Copies the problem tables from the handle's pinned host copy to the device
- * again (after the host copy changed, or to time a cold start).  The
- * reference keeps its tables in host memory only; this has no counterpart
- * there beyond the table construction in Simulator::Simulator. */
+/* Copies every device table of the problem again from the handle's pinned
+ * host copies: the FP64 tables and, once the mixed-precision engine has run
+ * on the handle, its FP32 tables (to time a cold start, or after the host
+ * copy changed).  The reference keeps its tables in host memory only; this
+ * has no counterpart there beyond the table construction in
+ * Simulator::Simulator. */
 mc_status mc_problem_upload(mc_problem *p);
 
-/* Bytes of the device copy of the problem tables (what mc_problem_upload
- * moves host -> device). */
+/* Bytes of the device tables of the problem (what mc_problem_upload moves
+ * host -> device). */
 mc_status mc_problem_table_bytes(const mc_problem *p, uint64_t *bytes);
 
 /* Releases a handle (the reference's Simulator destructor). */

@@ -86,6 +86,7 @@ mc_status mc_problem_upload(mc_problem *p)
     if (!p->dev.ready) return fail(p, MC_ERR_ARG, "problem was not loaded");
     std::string err;
     mc_status s = upload_tables(p->dev, err);
+    if (s == MC_OK) s = event_tables_upload(p->dev, err);
     if (s != MC_OK) p->err = err;
     return s;
 }
@@ -93,7 +94,7 @@ mc_status mc_problem_upload(mc_problem *p)
 mc_status mc_problem_table_bytes(const mc_problem *p, uint64_t *bytes)
 {
     if (!p || !bytes) return MC_ERR_ARG;
-    *bytes = (uint64_t)p->dev.blob_bytes;
+    *bytes = (uint64_t)(p->dev.blob_bytes + event_table_bytes(p->dev));
     return MC_OK;
 }
 

@@ -66,6 +66,10 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
                     const mc_tune *tune, std::string &err);
 void event_state_free(EventState *s);
 bool event_tables_ready(const Tables &t, DeviceProblem &d, std::string &err);
+// copies the mixed-precision engine's tables again from pinned host memory
+// (nothing before that engine first ran) and their size in bytes
+mc_status event_tables_upload(DeviceProblem &d, std::string &err);
+size_t event_table_bytes(const DeviceProblem &d);
 
 // batches (mc_event.cu)
 // sums_to (nullable): 2 device arrays per problem (sum, sumsq) to fold into

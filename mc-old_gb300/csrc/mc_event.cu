@@ -53,6 +53,8 @@ using namespace ev;
 struct EventState {
     EvHost host;
     void *d_blob = nullptr;
+    void *h_blob = nullptr;       // pinned copy of host.blob: mc_problem_upload copies it again
+    size_t blob_bytes = 0;
     EvTables dv{};
     DevBuf acc, mask, ovf, misc;
     int grid = 0, block = 0, tile = 0, ovf_cap = 0;
@@ -64,6 +66,7 @@ void event_state_free(EventState *s)
 {
     if (!s) return;
     if (s->d_blob) cudaFree(s->d_blob);
+    if (s->h_blob) cudaFreeHost(s->h_blob);
     devbuf_free(s->acc);
     devbuf_free(s->mask);
     devbuf_free(s->ovf);
@@ -108,17 +111,41 @@ bool event_tables_ready(const Tables &t, DeviceProblem &d, std::string &err)
     EventState *S = new EventState();
     if (!build_event_tables(t, S->host, err)) { delete S; return false; }
     cudaError_t e;
-    if ((e = cudaMalloc(&S->d_blob, S->host.blob.size())) != cudaSuccess) {
-        delete S;
-        err = cuda_msg(e, "cudaMalloc(event tables)");
+    S->blob_bytes = std::max<size_t>(S->host.blob.size(), 16);
+    S->host.blob.resize(S->blob_bytes);
+    if ((e = cudaMalloc(&S->d_blob, S->blob_bytes)) != cudaSuccess ||
+        (e = cudaHostAlloc(&S->h_blob, S->blob_bytes, cudaHostAllocDefault)) != cudaSuccess) {
+        event_state_free(S);
+        err = cuda_msg(e, "allocating the event tables");
         return false;
     }
-    cudaMemcpy(S->d_blob, S->host.blob.data(), S->host.blob.size(), cudaMemcpyHostToDevice);
+    std::memcpy(S->h_blob, S->host.blob.data(), S->blob_bytes);
+    if ((e = cudaMemcpyAsync(S->d_blob, S->h_blob, S->blob_bytes, cudaMemcpyHostToDevice, d.stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(d.stream)) != cudaSuccess) {
+        event_state_free(S);
+        err = cuda_msg(e, "uploading the event tables");
+        return false;
+    }
     for (auto &f : S->host.fix) *f.first = static_cast<const char *>(S->d_blob) + f.second;
     S->dv = S->host.view;
     d.ev_state = S;
     return true;
 }
+
+mc_status event_tables_upload(DeviceProblem &d, std::string &err)
+{
+    if (!d.ev_state) return MC_OK;   // the mixed-precision engine has not run yet
+    const EventState &S = *d.ev_state;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(S.d_blob, S.h_blob, S.blob_bytes, cudaMemcpyHostToDevice, d.stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(d.stream)) != cudaSuccess) {
+        err = cuda_msg(e, "upload event tables");
+        return MC_ERR_CUDA;
+    }
+    return MC_OK;
+}
+
+size_t event_table_bytes(const DeviceProblem &d) { return d.ev_state ? d.ev_state->blob_bytes : 0; }
 
 const EvTables &event_tables_view(const DeviceProblem &d) { return d.ev_state->dv; }
 

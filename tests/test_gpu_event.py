@@ -153,3 +153,22 @@ def test_event_overflow_is_a_status(mc):
         p.reset()
         p.run(n=100, mode="event")
         p.close()
+
+
+def test_upload_recopies_the_mixed_engine_tables(mc):
+    """mc_problem_upload copies the FP32 event tables again once the mixed
+    engine has built them (the end-to-end timing moves them every step); the
+    re-copied tables give the same tracks."""
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case("ce_sphere_small", d)
+        p = mc.Problem(d, d + "/xs_library")
+        b0 = p.table_bytes()
+        c1 = p.run(n=20000, mode="event", kernel=2)
+        b1 = p.table_bytes()
+        assert b1 > b0
+        p.upload()
+        p.reset()
+        c2 = p.run(n=20000, mode="event", kernel=2)
+        p.close()
+    for k in ("flights", "collisions", "crossings", "tally_updates", "freegas_iters"):
+        assert c1[k] == c2[k], k
