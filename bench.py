@@ -416,6 +416,7 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
         sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
         sampler.start()
         ms, launches, foms = 0.0, 0, []
+        cnt_sum = {}
         for k in range(a.steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -424,6 +425,8 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
             c = b.run(seed=SEED + k)
             ms += c["total_ms"]
             launches += c["launches"]
+            for key in ("flights", "collisions", "crossings", "tally_updates", "xs_evals", "particles"):
+                cnt_sum[key] = cnt_sum.get(key, 0) + c[key]
         clocks = sampler.stop()
         T = ms / a.steps * 1e-3
         for p in probs:
@@ -432,10 +435,34 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
             if tot > 0:
                 err = float(np.sqrt(np.sum(s ** 2))) / tot
                 foms.append(1.0 / (err * err * T))
+        # e2e through the C ABI: every problem's tables uploaded again from
+        # pinned host memory, the batch run, every problem's tallies read back
+        e2e_t = 0.0
+        h2d = int(sum(p.table_bytes() for p in probs))
+        d2h = 0
+        for k in range(a.e2e_steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for p in probs:
+                p.upload()
+                p.reset()
+            b.run(seed=SEED + 100 + k)
+            d2h = 0
+            for p in probs:
+                tot = p.all_tallies()
+                d2h += int(sum(x.nbytes for x in tot[2:]))
+            e2e_t += time.perf_counter() - t0
         b.close()
         for p in probs:
             p.close()
     total = sum(hist)
+    peaks, peak_kind = _measured_peaks()
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    # multigroup: one 4-byte table value per cross-section evaluation (the
+    # scatter-CDF probes are not counted), one FP64 update per tally update
+    alg_bytes = (4 * cnt_sum.get("xs_evals", 0) + 16 * cnt_sum.get("tally_updates", 0)) / a.steps
+    achieved = alg_bytes / T / 1e9
     line = {"metric": METRIC, "value": total / T, "unit": "histories/s", "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": T * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "dtype_detail": "f32 tracking, f64 tally accumulation",
@@ -448,6 +475,13 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
             "fom_per_problem": {"median": float(np.median(foms)), "min": float(np.min(foms)),
                                 "max": float(np.max(foms)), "unit": "1/s",
                                 "tally": "total leakage, R over the group bins, T = whole-batch latency"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if peak else None, "traffic": None,
+                         "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs",
+                         "algorithmic_bytes_per_step": alg_bytes},
+            "counters_per_step": {k: v / a.steps for k, v in cnt_sum.items()},
+            "e2e": {"value": total * a.e2e_steps / e2e_t if a.e2e_steps else None, "unit": "histories/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clocks, "gpu_launches": launches}
     if rank == 0:
         print(json.dumps(line))
