@@ -407,11 +407,20 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
         probs = [mcgpu.Problem(d) for d, _ in specs]
         hist = [h for _, h in specs]
         b = mcgpu.Batch(probs, hist)
-        tuned = b.autotune(seed=SEED + 17, fraction=0.01)
+        run_kw = {}
+        if a.kernel == "auto":
+            tuned = b.autotune(seed=SEED + 17, fraction=0.01)
+        else:   # a fixed shape (profiling runs)
+            mb = a.blocks_per_sm if a.blocks_per_sm is not None else (2 if a.kernel == "tile" else 8)
+            tuned = {"kernel": 1 if a.kernel == "tile" else 2, "blocks_per_sm": mb,
+                     "bank_capacity": a.tile if a.kernel == "tile" else 0}
+            run_kw = dict(kernel=tuned["kernel"], blocks_per_sm=mb)
+            if a.kernel == "tile":
+                run_kw["bank_capacity"] = a.tile
         for w in range(a.warmup):
             for p in probs:
                 p.reset()
-            b.run(seed=SEED + 1000 + w)
+            b.run(seed=SEED + 1000 + w, **run_kw)
         torch.cuda.synchronize()
         sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
         sampler.start()
@@ -422,7 +431,7 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
             torch.cuda.synchronize()
             for p in probs:
                 p.reset()
-            c = b.run(seed=SEED + k)
+            c = b.run(seed=SEED + k, **run_kw)
             ms += c["total_ms"]
             launches += c["launches"]
             for key in ("flights", "collisions", "crossings", "tally_updates", "xs_evals", "particles"):
@@ -447,7 +456,7 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
             for p in probs:
                 p.upload()
                 p.reset()
-            b.run(seed=SEED + 100 + k)
+            b.run(seed=SEED + 100 + k, **run_kw)
             d2h = 0
             for p in probs:
                 tot = p.all_tallies()
