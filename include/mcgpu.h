@@ -82,6 +82,11 @@ typedef struct {
     uint32_t max_events;     /* events one particle may take before the run stops
                                 with MC_ERR_TIMEOUT (0 = 2^22); a small cap
                                 exercises that path on purpose */
+    uint32_t refill;         /* per-thread event kernel: a lane that finished its
+                                history waits until this many lanes of its warp
+                                are idle, so that they fold and start histories
+                                together (1..32; 0 = 8 for multigroup problems,
+                                4 otherwise) */
 } mc_tune;
 
 /* Event counters and timing of the last mc_run.  The counts follow the

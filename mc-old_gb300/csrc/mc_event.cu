@@ -156,6 +156,7 @@ struct EvLaunch {
     int ovf_cap = 0;        // split-copy slots per CTA
     int flavor = FL_ALL;    // per-thread kernel flavour (FL_ALL / FL_CE / FL_MG)
     uint32_t max_events = kMaxEvents;
+    int refill = 1;         // k_track: idle lanes a warp gathers before it starts histories
     size_t smem = 0;
 };
 
@@ -164,6 +165,11 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
                                     std::string &err)
 {
     L.flavor = flavor;
+    // measured: 4 idle lanes for continuous-energy histories (~115 events),
+    // 8 for the short multigroup ones
+    const int refill_default = flavor == FL_MG ? 8 : 4;
+    L.refill = (tune && tune->refill) ? (int)tune->refill : (tuned.refill ? (int)tuned.refill : refill_default);
+    if (L.refill < 1 || L.refill > 32) { err = "refill must be 1..32"; return MC_ERR_ARG; }
     L.kernel = (tune && tune->kernel) ? (int)tune->kernel : (tuned.kernel ? (int)tuned.kernel : 2);
     if (L.kernel < 1 || L.kernel > 2) { err = "kernel must be 1 (tile) or 2 (per thread)"; return MC_ERR_ARG; }
     if (comb_teeth > 0 && L.kernel != 2) {
@@ -301,6 +307,7 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     A.smem_sums = smem_sums ? 1 : 0;
     A.comb_bank_max = comb ? t.comb_bank_max : 0;
     A.comb_teeth = comb;
+    A.refill_min = L.refill;
     A.n_prob = 0;
     cudaEventRecord(d.ev[0], d.stream);
     pick_kernel(L.minb, false, L.kernel, L.flavor)<<<L.grid, L.block, L.smem, d.stream>>>(V, A);
@@ -452,7 +459,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     L.max_events = (tune && tune->max_events) ? tune->max_events : kMaxEvents;
     const bool same_shape = b->have_shape && L.grid == b->shape.grid && L.tile == b->shape.tile &&
                             L.minb == b->shape.minb && L.kernel == b->shape.kernel &&
-                            L.max_events == b->shape.max_events;
+                            L.max_events == b->shape.max_events && L.refill == b->shape.refill;
     for (uint32_t i = 0; i < n; ++i) b->h_seeds[i] = batch_problem_seed(seed, i);
     char *m = static_cast<char *>(b->meta.ptr);
     size_t off = 0;
@@ -482,6 +489,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         A.ovf_cap = L.ovf_cap;
         A.tile = L.tile;
         A.smem_sums = 0;
+        A.refill_min = L.refill;
         A.tabs = d_tabs;
         A.prefix = d_prefix;
         A.seeds = d_seeds;

@@ -39,6 +39,7 @@ struct EvArgs {
     int tile;
     int smem_sums;                // per-CTA sums live in shared memory
     int comb_bank_max, comb_teeth;  // particle comb on the per-thread stack (0 teeth: off)
+    int refill_min;               // k_track: idle lanes a warp gathers before it starts histories
     // batch of problems (kBatch): history index space = concatenation of
     // every problem's histories
     const EvTables *tabs;         // [n_prob]
@@ -1595,11 +1596,18 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
             C.cnt[C_PART]++;
             if (++walks > (1u << 24)) atomicCAS(&s_status, 0, DS_TIMEOUT);
         }
-        if (!have && open) {
+        // new histories start together: a lane whose history ended waits
+        // until refill_min lanes of its warp are idle (or no lane has work
+        // left), so the fold and the source sampling run for many lanes at
+        // once instead of for one or two while the rest wait
+        const bool idle = !have && !exhausted;
+        const unsigned im = __ballot_sync(0xffffffffu, idle);
+        const bool refill = __popc(im) >= A.refill_min || __ballot_sync(0xffffffffu, have) == 0u;
+        if (refill && !have && open) {
             history_fold<kFl>(C, hslot, prob);
             open = false;
         }
-        const bool need = !have && !exhausted;
+        const bool need = refill && idle;
         if constexpr (!kBatch) {
             const unsigned m = __ballot_sync(0xffffffffu, need);
             if (m) {

@@ -47,7 +47,7 @@ class Tune(ctypes.Structure):
                 ("stack_depth", ctypes.c_uint32), ("chunk", ctypes.c_uint32),
                 ("bank_capacity", ctypes.c_uint32), ("record_digests", ctypes.c_uint32),
                 ("blocks_per_sm", ctypes.c_uint32), ("kernel", ctypes.c_uint32),
-                ("max_events", ctypes.c_uint32)]
+                ("max_events", ctypes.c_uint32), ("refill", ctypes.c_uint32)]
 
 
 class Counters(ctypes.Structure):

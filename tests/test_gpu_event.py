@@ -172,3 +172,27 @@ def test_upload_recopies_the_mixed_engine_tables(mc):
         p.close()
     for k in ("flights", "collisions", "crossings", "tally_updates", "freegas_iters"):
         assert c1[k] == c2[k], k
+
+
+@pytest.mark.parametrize("case", ["ce_sphere_small", "slab_features"])
+def test_refill_threshold_keeps_every_track(mc, case):
+    """mc_tune.refill only changes when a warp's idle lanes take new
+    histories: every history keeps its own random stream, so the event
+    counts are identical for any threshold, and every history runs once."""
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case(case, d)
+        p = mc.Problem(d, d + "/xs_library")
+        out = []
+        for r in (1, 4, 32):
+            p.reset()
+            c = p.run(n=30000, mode="event", kernel=2, refill=r)
+            out.append((c, p.all_tallies()[2]))
+        with pytest.raises(mc.McError):
+            p.run(n=10, mode="event", kernel=2, refill=33)
+        p.close()
+    (c0, s0) = out[0]
+    for c, s in out[1:]:
+        assert c["histories"] == 30000
+        for k in ("flights", "collisions", "crossings", "tally_updates", "particles", "splits", "freegas_iters"):
+            assert c[k] == c0[k], k
+        assert np.allclose(s, s0, rtol=1e-9, atol=1e-14)
