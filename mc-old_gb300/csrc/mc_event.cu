@@ -305,8 +305,6 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     A.sq = d.d_sq;
     A.tile = L.tile;
     A.smem_sums = smem_sums ? 1 : 0;
-    A.comb_bank_max = comb ? t.comb_bank_max : 0;
-    A.comb_teeth = comb;
     A.refill_min = L.refill;
     A.n_prob = 0;
     cudaEventRecord(d.ev[0], d.stream);
@@ -359,6 +357,7 @@ struct BatchState {
     bool have_shape = false;
     bool count_histories = true;      // false for autotuning batches
     int flavor = FL_ALL;              // per-thread kernel flavour for the whole batch
+    int comb_teeth = 0;               // most comb teeth of any problem (stack depth)
     mc_counters last{};
 };
 
@@ -391,12 +390,6 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
     std::vector<unsigned long long> prefix(n + 1, 0);
     std::vector<double *> psum(n), psq(n);
     for (uint32_t i = 0; i < n; ++i) {
-        if (tabs[i]->comb_teeth > 0) {
-            // a lane of the batch kernel keeps no comb state per problem
-            batch_state_free(b);
-            err = "problem " + std::to_string(i) + ": batches do not run the particle comb (mc_run does)";
-            return MC_ERR_INPUT;
-        }
         if (!event_tables_ready(*tabs[i], *probs[i], err)) { batch_state_free(b); err = "problem " + std::to_string(i) + ": " + err; return MC_ERR_INPUT; }
         views[i] = probs[i]->ev_state->dv;
         prefix[i + 1] = prefix[i] + hist[i];
@@ -407,11 +400,13 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
     }
     // one flavour for the launch: every problem multigroup (or every one
     // continuous energy) and none with a time filter, else the full kernel
+    // (the particle comb, too, takes the full kernel)
     bool all_mg = true, all_ce = true, any_time = false;
     for (uint32_t i = 0; i < n; ++i) {
         all_mg = all_mg && views[i].G > 0;
         all_ce = all_ce && views[i].G == 0;
-        any_time = any_time || views[i].has_time;
+        any_time = any_time || views[i].has_time || views[i].comb_teeth > 0;
+        b->comb_teeth = std::max(b->comb_teeth, views[i].comb_teeth);
     }
     b->flavor = any_time ? FL_ALL : (all_mg ? FL_MG : (all_ce ? FL_CE : FL_ALL));
     b->total = prefix[n];
@@ -453,7 +448,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     DeviceProblem shape_dev;
     shape_dev.sms = device_sms;
     EvLaunch L;
-    mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, b->flavor, 0, L, err);
+    mc_status st = event_launch_shape(shape_dev, tune, tuned, 0, true, b->flavor, b->comb_teeth, L, err);
     if (st != MC_OK) return st;
     if ((st = event_scratch(b->scratch, b->stream, L.grid, L.tile, L.ovf_cap, b->row_nb, err)) != MC_OK) return st;
     L.max_events = (tune && tune->max_events) ? tune->max_events : kMaxEvents;

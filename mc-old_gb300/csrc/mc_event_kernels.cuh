@@ -38,7 +38,6 @@ struct EvArgs {
     int *status;
     int tile;
     int smem_sums;                // per-CTA sums live in shared memory
-    int comb_bank_max, comb_teeth;  // particle comb on the per-thread stack (0 teeth: off)
     int refill_min;               // k_track: idle lanes a warp gathers before it starts histories
     // batch of problems (kBatch): history index space = concatenation of
     // every problem's histories
@@ -1580,10 +1579,13 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
         return true;
     };
     for (uint32_t it = 1;; ++it) {
-        if constexpr (kFl == FL_ALL && !kBatch) {
+        if constexpr (kFl == FL_ALL) {
             // a walk has just ended whenever the stack is non-empty here
-            if (!have && A.comb_teeth > 0 && sp >= A.comb_bank_max)
-                sp = comb_stack(stk, sp, A.comb_teeth, A.seed, hist, p.id);
+            if (!have && sp > 0) {
+                const EvTables &Vc = tab(prob);
+                if (Vc.comb_teeth > 0 && sp >= Vc.comb_bank_max)
+                    sp = comb_stack(stk, sp, Vc.comb_teeth, seed_of(prob), hist, p.id);
+            }
         }
         // the next particle: the history's own split copies first (LIFO, as
         // the reference's bank), then a new history

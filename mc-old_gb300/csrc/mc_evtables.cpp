@@ -237,6 +237,8 @@ bool build_event_tables(const Tables &t, EvHost &h, std::string &err)
     P.add(t.src_group, &V.src_group);
     V.wr = (float)t.wr;
     V.ws = (float)t.ws;
+    V.comb_bank_max = t.comb_teeth > 0 ? t.comb_bank_max : 0;
+    V.comb_teeth = t.comb_teeth > 0 ? t.comb_teeth : 0;
     return true;
 }
 

@@ -74,6 +74,7 @@ struct EvTables {
     const float *src_pos, *src_dir_par, *src_e_par, *src_cdf;
     const int *src_cell, *src_dir_kind, *src_e_kind, *src_group;
     float wr, ws;
+    int comb_bank_max, comb_teeth;    // particle comb (0 teeth: off)
 };
 
 // Host-side storage behind EvTables (one packed device allocation).

@@ -5,9 +5,9 @@ kernel, each of which keeps one history's bank.  Replay reproduces the
 oracle's event digests and tally sums bit for bit for several (bank_max,
 teeth) pairs.  The oracle's comb is pinned to the compiled reference's own
 particle_comb by the comb_slab golden fixture.  Plain FP64 and the mixed
-per-thread kernel agree with replay statistically.  The tile kernel and
-batches refuse a combed problem with a status, because they keep no
-per-history bank."""
+per-thread kernel agree with replay statistically, and a batch runs every
+combed problem as its lone run does.  The tile kernel refuses a combed
+problem with a status, because it keeps no per-history bank."""
 import tempfile
 
 import numpy as np
@@ -106,8 +106,47 @@ def test_comb_refused_where_no_history_bank_exists(mc):
         with pytest.raises(mc.McError) as e:
             p.run(mode="event", kernel=1)
         assert e.value.status == 8 and "comb" in str(e.value)    # MC_ERR_ARG
+        b = mc.Batch([p], [100])
         with pytest.raises(mc.McError) as e:
-            mc.Batch([p], [100])
-        assert e.value.status == 1 and "comb" in str(e.value)
+            b.run(seed=3, kernel=1)
+        assert e.value.status == 8 and "comb" in str(e.value)
+        b.close()
         p.run(n=50, mode="replay")     # the handle stays usable
         p.close()
+
+
+def test_comb_in_a_batch_equals_lone_runs(mc):
+    """A batch mixing combed problems (different bank_max / teeth) with an
+    uncombed one: problem i follows the histories of its lone run with seed
+    batch_problem_seed(seed, i), so the event counts of the whole batch
+    equal the sum of the lone runs' and every tally agrees."""
+    import os
+    seed = 4242
+    settings = [(3, 2), (1, 1), (6, 4), None]
+    hist = [3000, 2000, 2500, 1500]
+    with tempfile.TemporaryDirectory() as root:
+        probs = []
+        for k, st in enumerate(settings):
+            d = os.path.join(root, "p%d" % k)
+            os.makedirs(d)
+            if st is None:
+                cases.write_case("slab_features", d)
+            else:
+                cases.comb_slab(d, samples=hist[k], bank_max=st[0], teeth=st[1])
+            probs.append(mc.Problem(d, d + "/xs_library"))
+        b = mc.Batch(probs, hist)
+        cb = b.run(seed=seed)
+        assert cb["histories"] == sum(hist)
+        res = [p.all_tallies() for p in probs]
+        b.close()
+        tot = {}
+        for i, p in enumerate(probs):
+            p.reset()
+            c = p.run(n=hist[i], seed=mc.batch_problem_seed(seed, i), mode="event")
+            for k in ("flights", "collisions", "crossings", "tally_updates", "particles", "splits"):
+                tot[k] = tot.get(k, 0) + c[k]
+            m2, s2, su2, _ = p.all_tallies()
+            assert np.allclose(res[i][2], su2, rtol=1e-6, atol=1e-12), f"problem {i}"
+            p.close()
+    for k, v in tot.items():
+        assert cb[k] == v, k
