@@ -196,3 +196,21 @@ def test_refill_threshold_keeps_every_track(mc, case):
         for k in ("flights", "collisions", "crossings", "tally_updates", "particles", "splits", "freegas_iters"):
             assert c[k] == c0[k], k
         assert np.allclose(s, s0, rtol=1e-9, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["ce_sphere_small", "slab_features", "quadrics", "absorber_slab", "comb_slab"])
+def test_event_agrees_with_the_reference_run(mc, name):
+    """The mixed mode against the compiled reference's own output for the
+    same input (the golden fixtures: means and uncertainties the reference
+    wrote), with the reference's history count and an independent random
+    stream: every bin within combined 3 sigma, chi-square consistent."""
+    from helpers import golden_arrays, load_golden
+    g = load_golden(name)
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case(name, d)
+        p = mc.Problem(d, d + "/xs_library")
+        p.run(n=g["nsample"], seed=g["seed"] + 1000, mode="event")
+        m, s, _, _ = p.all_tallies()
+        p.close()
+    gm, gu = golden_arrays(g)
+    assert_agree(m, s, gm, gu, f"{name}: mixed mode vs the reference")
