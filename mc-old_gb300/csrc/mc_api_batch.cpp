@@ -142,7 +142,11 @@ mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double frac, mc_tune *ou
         b->err = "cannot allocate autotune tallies";
         return MC_ERR_NOMEM;
     }
-    cudaMemset(pool, 0, 2 * total_bins * sizeof(double));
+    if (cudaMemset(pool, 0, 2 * total_bins * sizeof(double)) != cudaSuccess) {
+        cudaFree(pool);
+        b->err = "cannot clear autotune tallies";
+        return MC_ERR_CUDA;
+    }
     std::vector<double *> sums;
     size_t off = 0;
     for (uint32_t i = 0; i < n; ++i) {

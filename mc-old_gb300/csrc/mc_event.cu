@@ -425,9 +425,11 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
     }
     char *m = static_cast<char *>(b->meta.ptr);
     size_t off = 0;
+    cudaError_t put_err = cudaSuccess;
     auto put = [&](const void *src, size_t bytes) {
         off = (off + 255) & ~(size_t)255;
-        cudaMemcpy(m + off, src, bytes, cudaMemcpyHostToDevice);
+        const cudaError_t e = cudaMemcpy(m + off, src, bytes, cudaMemcpyHostToDevice);
+        if (put_err == cudaSuccess) put_err = e;
         const size_t at = off;
         off += bytes;
         return at;
@@ -436,6 +438,11 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
     put(prefix.data(), (n + 1) * 8);
     put(psum.data(), n * sizeof(double *));
     put(psq.data(), n * sizeof(double *));
+    if (put_err != cudaSuccess) {
+        batch_state_free(b);
+        err = cuda_msg(put_err, "batch descriptors");
+        return MC_ERR_CUDA;
+    }
     b->count_histories = sums_to == nullptr;
     *out = b;
     return MC_OK;
