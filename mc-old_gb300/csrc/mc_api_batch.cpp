@@ -36,8 +36,13 @@ mc_status mc_autotune(mc_problem *p, uint64_t sample, uint64_t seed, mc_tune *ou
 {
     if (!p || !out) return MC_ERR_ARG;
     if (!p->dev.ready) { p->err = "problem was not loaded"; return MC_ERR_ARG; }
-    if (sample == 0) sample = 200000;
     DeviceProblem &d = p->dev;
+    // every candidate shape must be timed with work for all of its threads:
+    // at least 4 histories per thread of the largest grid (8 CTAs of 128
+    // threads per SM)
+    const uint64_t per_thread = 8ull * 128ull * (uint64_t)std::max(d.sms, 1);
+    if (sample == 0) sample = 8 * per_thread;
+    sample = std::max<uint64_t>(sample, 4 * per_thread);
     const size_t nb = (size_t)std::max<long long>(d.dt.n_bins, 1);
     double *tmp = nullptr;
     if (cudaMalloc(&tmp, 2 * nb * sizeof(double)) != cudaSuccess) {

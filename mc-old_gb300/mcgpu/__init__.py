@@ -280,8 +280,9 @@ class Problem:
         return (d[: nb * K].reshape(nb, K), s[: nb * K].reshape(nb, K),
                 r[: nb * M].reshape(nb, M), rs[: nb * M].reshape(nb, M))
 
-    def autotune(self, sample: int = 200000, seed: int = DEFAULT_SEED) -> dict:
-        """Pick and keep the event engine's fastest launch shape."""
+    def autotune(self, sample: int = 0, seed: int = DEFAULT_SEED) -> dict:
+        """Pick and keep the event engine's fastest launch shape (sample 0:
+        the library's default, 8 histories per thread of the largest shape)."""
         t = Tune()
         self._check(lib().mc_autotune(self._h, sample, seed, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
