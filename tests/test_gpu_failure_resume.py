@@ -72,3 +72,24 @@ def test_checkpoint_resume_is_bit_exact_in_replay(mc):
         c.close()
     for x, y in zip(ref, got):
         assert same_bits(x, y)
+
+
+def test_event_cap_in_a_batch_is_a_status_and_the_batch_recovers(mc):
+    """The batch launch reports an exceeded event budget as MC_ERR_TIMEOUT;
+    the next run (a new graph with the default budget) completes."""
+    import mcgpu.workloads as W
+    with tempfile.TemporaryDirectory() as root:
+        specs = W.batch_shields(root, n_problems=8, min_hist=1000, max_hist=3000)
+        probs = [mc.Problem(d) for d, _ in specs]
+        hist = [h for _, h in specs]
+        b = mc.Batch(probs, hist)
+        with pytest.raises(mc.McError) as e:
+            b.run(seed=9, max_events=1)
+        assert e.value.status == 5          # MC_ERR_TIMEOUT
+        for p in probs:
+            p.reset()
+        c = b.run(seed=9)
+        assert c["histories"] == sum(hist)
+        b.close()
+        for p in probs:
+            p.close()
