@@ -116,3 +116,33 @@ def test_command_line_driver_reports_input_errors(L):
         r = subprocess.run([exe, d], capture_output=True, text=True, timeout=60)
     assert r.returncode == 2 + 1, r.stdout + r.stderr      # MC_ERR_INPUT, before any device use
     assert "[ERROR] setup" in r.stderr
+
+
+def test_header_is_plain_c_and_the_ctypes_structs_match_it():
+    """include/mcgpu.h compiles as pedantic C99, and the Python layer's
+    ctypes copies of mc_tune and mc_counters have the header's size and
+    field offsets (a field added on one side only would shift the rest)."""
+    import subprocess
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "mc-old_gb300"))
+    import mcgpu
+    structs = {"mc_tune": mcgpu.Tune, "mc_counters": mcgpu.Counters}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "mcgpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["return 0;", "}"]
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "layout.c"), os.path.join(d, "layout")
+        with open(src, "w") as fh:
+            fh.write("\n".join(lines) + "\n")
+        r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                            "-I", os.path.join(ROOT, "include"), src, "-o", exe], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    got = dict(zip(out[0::2], (int(x) for x in out[1::2])))
+    for cname, py in structs.items():
+        assert got[cname] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[f"{cname}.{f}"] == getattr(py, f).offset, f"{cname}.{f}"
