@@ -26,7 +26,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+# MC_ORACLE_LIB names another build of the same source (the sanitizer build)
+LIB_PATH = os.environ.get("MC_ORACLE_LIB") or os.path.join(HERE, "_build", "liboracle.so")
 
 # enums of mc_oracle.h
 PX, PY, PZ, PLANE, SPHERE, CYLX, CYLY, CYLZ = range(8)
