@@ -31,6 +31,9 @@ roofline_l2  the same algorithmic bytes against an L2 read bandwidth measured
            in the run (the tables are L2-resident).
 cpu_baseline  the CPU oracle (a C restatement of the reference's history loop)
            on the host cores, on a bounded sample of the same workload.
+plain_fp64 the plain FP64 GPU history path (MC_FP64_PLAIN) on the same
+           workload after the timed region: histories/s, FOM and the
+           mixed / plain FOM ratio.
 
 --impl reference times that CPU implementation (all host threads) as the
 reference arm and prints its own JSON line.
@@ -332,6 +335,20 @@ def gpu_arm(a):
             tot = prob.all_tallies()
             e2e_t += time.perf_counter() - t0
             d2h = int(sum(x.nbytes for x in tot[2:]))
+        # the plain FP64 GPU history path on the same problem, for the
+        # metric's "vs plain FP64" (after the timed region, rank 0 only)
+        plain = None
+        if a.mode == "event" and a.plain_histories > 0 and rank == 0:
+            Hp = a.plain_histories
+            prob.reset()
+            prob.run(n=min(Hp, 20000), first=10**11, seed=SEED, mode="plain")
+            prob.reset()
+            cp = prob.run(n=Hp, first=10**11 + Hp, seed=SEED, mode="plain")
+            mp, sp, _, _ = prob.tally(prob.names.index("leakage"))
+            Tp = cp["total_ms"] * 1e-3
+            fom_p = 1.0 / ((sp[0] / mp[0]) ** 2 * Tp) if mp[0] > 0 else None
+            plain = {"value": Hp / Tp, "unit": "histories/s", "histories": Hp, "fom": fom_p,
+                     "note": "MC_FP64_PLAIN on the same workload: FP64 tracking, native FP64 math"}
         prob.close()
 
     value_local = a.steps * H / (dev_ms * 1e-3)
@@ -394,6 +411,10 @@ def gpu_arm(a):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if plain:
+        fom_m = line["fom"]["value"]
+        plain["fom_ratio"] = fom_m / plain["fom"] if (fom_m and plain["fom"]) else None
+        line["plain_fp64"] = plain
     print(json.dumps(line))
     return 0
 
@@ -514,6 +535,8 @@ def main():
     ap.add_argument("--tile", type=int, default=512)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-histories", type=int, default=4000)
+    ap.add_argument("--plain-histories", type=int, default=500_000,
+                    help="histories of the plain FP64 comparison run (0: skip)")
     ap.add_argument("--ref-histories-per-proc", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     a = ap.parse_args()
