@@ -29,6 +29,9 @@ roofline   the transport kernels against HBM: algorithmic bytes per run =
            MEASURED_PEAKS.json hbm_gbs; traffic from the committed ncu summary.
 roofline_l2  the same algorithmic bytes against an L2 read bandwidth measured
            in the run (the tables are L2-resident).
+roofline_issue  the kernel against its issue bound: warp instructions per
+           history from the committed ncu capture of the same launch shape
+           x histories/s, over 4 schedulers per SM x the sampled SM clock.
 cpu_baseline  the CPU oracle (a C restatement of the reference's history loop)
            on the host cores, on a bounded sample of the same workload.
 plain_fp64 the plain FP64 GPU history path (MC_FP64_PLAIN) on the same
@@ -188,6 +191,25 @@ def _ncu_traffic():
             return json.load(f)
     except OSError:
         return None
+
+
+def _issue_roofline(prof, tuned, hist_per_s, clocks, sms):
+    """The kernel against its issue bound: warp instructions per history
+    (smsp__inst_executed.sum of the committed full ncu capture of the same
+    launch shape) x histories/s, against 4 warp schedulers per SM, each
+    issuing one instruction per cycle, at the SM clock sampled during the
+    timed region; None when no capture of this shape is committed."""
+    if not prof or not tuned or tuned.get("kernel") != 2:
+        return None
+    ipt = prof.get("issue:k_track:%d" % tuned["blocks_per_sm"])
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if not ipt or not mhz:
+        return None
+    peak = sms * 4 * mhz * 1e6
+    achieved = ipt * hist_per_s
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+            "frac": achieved / peak, "warp_instructions_per_history": ipt,
+            "peak_source": f"{sms} SMs x 4 schedulers x {mhz:.0f} MHz (sampled)"}
 
 
 def make_workload(tmp: str, histories: int) -> str:
@@ -399,6 +421,8 @@ def gpu_arm(a):
                      "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs",
                      "algorithmic_bytes_per_step": alg_bytes / a.steps,
                      "kernel_ms_per_step": transport_ms / a.steps},
+        "roofline_issue": _issue_roofline(traffic, tuned, value_local, clocks,
+                                          torch.cuda.get_device_properties(0).multi_processor_count),
         "roofline_l2": {"bound": "l2", "achieved": achieved, "peak": l2_peak, "unit": "GB/s",
                         "frac": achieved / l2_peak if l2_peak else None,
                         "peak_source": "measured in this run: one reduction kernel reading a 32 MiB L2-resident buffer 64 times"},

@@ -22,3 +22,16 @@ def test_reference_arm_prints_one_contract_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert "ce_sphere" in line["config"]["workload"]
+
+
+def test_issue_roofline_arithmetic():
+    """roofline_issue = committed warp instructions per history x histories/s
+    over 4 schedulers per SM x SM clock; absent for shapes without a capture."""
+    sys.path.insert(0, ROOT)
+    import bench
+    prof = {"issue:k_track:6": 6000.0}
+    r = bench._issue_roofline(prof, {"kernel": 2, "blocks_per_sm": 6}, 1e8, {"sm_mhz": 2000.0}, 150)
+    assert r["bound"] == "issue" and abs(r["peak"] - 150 * 4 * 2e9) < 1
+    assert abs(r["achieved"] - 6e11) < 1 and abs(r["frac"] - 0.5) < 1e-12
+    assert bench._issue_roofline(prof, {"kernel": 2, "blocks_per_sm": 8}, 1e8, {"sm_mhz": 2000.0}, 150) is None
+    assert bench._issue_roofline(prof, {"kernel": 1, "blocks_per_sm": 2}, 1e8, {"sm_mhz": 2000.0}, 150) is None
