@@ -68,7 +68,9 @@ typedef struct {
     uint32_t grid_blocks;    /* blocks, 0 = fill the GPU */
     uint32_t stack_depth;    /* split-particle stack per thread: FP64 modes and the
                                 per-thread event kernel (0 = 32, or teeth + 32
-                                with the particle comb) */
+                                with the particle comb); the tile kernel: split
+                                copies its CTA's overflow bank holds (0 = 4 per
+                                tile particle) */
     uint32_t chunk;          /* FP64 modes: histories per fold chunk (0 = auto) */
     uint32_t bank_capacity;  /* event mode: particles per CTA tile (0 = tuned / 512) */
     uint32_t record_digests; /* FP64 modes: keep per-history event digests */
@@ -198,9 +200,15 @@ mc_status mc_report(const mc_problem *p, const char *path);
  * equal bit for bit to what mc_run in MC_FP64_REPLAY adds for the same
  * range; the handle's own tallies are not touched.  Problems with more tally
  * bins than the scratch holds are refused with MC_ERR_ARG.  The first call on
- * a device looks up the array's device address once; make that call before
- * any stream capture.  Every call shares the one array, so calls that overlap
- * on the GPU (two host threads, two handles) race; serialise them. */
+ * a device looks up the array's device address once and keeps it for the
+ * life of the process; make that call before any stream capture.  The kept
+ * address belongs to the device's primary context: after cudaDeviceReset (or
+ * after that context is released and created again) it is stale, so do not
+ * call this entry point again in that process.  The grid is 96 blocks of 128
+ * threads (the split stacks of every thread live in the fixed array), so
+ * throughput is below mc_run's replay.  Every call shares the one array, so
+ * calls that overlap on the GPU (two host threads, two handles) race;
+ * serialise them. */
 mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first_history, uint64_t n_histories,
                                 uint64_t seed, double *d_sum, double *d_sumsq);
 

@@ -24,6 +24,19 @@ mc_status status_from_device(int ds)
     }
 }
 
+const char *device_status_text(int ds)
+{
+    switch (ds) {
+    case DS_LOST: return "a particle was lost (no cell contains it)";
+    case DS_OVERFLOW: return "split stack or filter buffer overflow";
+    case DS_TIMEOUT:
+        return "a particle exceeded the event limit, a history its particle limit, or the free-gas loop its "
+               "candidate limit";
+    case DS_NAN: return "a non-finite track length, energy or weight";
+    default: return "device error status";
+    }
+}
+
 bool devbuf_reserve(DevBuf &buf, size_t bytes)
 {
     if (bytes <= buf.bytes && buf.ptr) return true;
@@ -289,9 +302,8 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
         t_transport += a;
         t_fold += b;
         if (hs != DS_OK) {
-            err = hs == DS_LOST ? "a particle was lost (no cell contains it)"
-                : hs == DS_OVERFLOW ? "split stack or filter buffer overflow (raise mc_tune.stack_depth)"
-                : "device error status";
+            err = device_status_text(hs);
+            if (hs == DS_OVERFLOW) err += " (raise mc_tune.stack_depth)";
             return status_from_device(hs);
         }
     }

@@ -85,6 +85,8 @@ const mc_counters &batch_counters(const BatchState *b);
 uint64_t batch_problem_seed(uint64_t seed, uint32_t i);
 
 mc_status status_from_device(int ds);
+// message for a device status word (DS_*) of the FP64 history kernels
+const char *device_status_text(int ds);
 void lr_scratch_free(void *lr);
 std::string cuda_msg(cudaError_t e, const char *what);
 

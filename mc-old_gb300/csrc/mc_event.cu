@@ -217,7 +217,14 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
             err = "tile (bank_capacity) must be a multiple of 256 up to 4096";
             return MC_ERR_ARG;
         }
-        L.ovf_cap = 4 * L.tile;
+        // split copies waiting in the CTA's overflow bank: stack_depth slots
+        // when given (a small bank exercises the overflow status), else 4 per
+        // tile particle
+        L.ovf_cap = (tune && tune->stack_depth) ? (int)tune->stack_depth : 4 * L.tile;
+        if (L.ovf_cap < 1 || L.ovf_cap > (1 << 20)) {
+            err = "stack_depth (the tile kernel's overflow bank) must be 1..2^20";
+            return MC_ERR_ARG;
+        }
         L.smem = tile_smem_bytes(L.tile, nb_smem);
     }
     EvKernel k = pick_kernel(L.minb, batch, L.kernel, L.flavor);

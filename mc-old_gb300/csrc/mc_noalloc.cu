@@ -25,7 +25,10 @@ namespace {
 
 constexpr size_t kScratchBytes = 64ull << 20;     // MC_NOALLOC_SCRATCH_BYTES
 constexpr size_t kCtrlBytes = 4096;
-constexpr int kThreads = 12288;                  // 96 blocks of 128
+// 96 blocks of 128: fewer CTAs than the GPU has SMs, because the split
+// stacks of every thread must fit the fixed array; this path trades
+// throughput against mc_run's replay for allocating nothing
+constexpr int kThreads = 12288;
 constexpr int kBlock = 128;
 constexpr uint32_t kDepth = 16;                  // split copies per history
 constexpr uint32_t kMinChunk = 1024;             // histories per fold, at least
@@ -96,9 +99,11 @@ extern "C" mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first, uint64
     const uint64_t chunk = (kScratchBytes - kCtrlBytes - stack_bytes) / row_bytes;
 
     // the array keeps the previous call's contents: clear what starts at zero
+    // (the caller's arrays hold exactly n_bins doubles, none when n_bins is 0)
+    const size_t out_bytes = (size_t)d.dt.n_bins * sizeof(double);
     if ((e = cudaMemsetAsync(b, 0, kCtrlBytes, d.stream)) != cudaSuccess ||
-        (e = cudaMemsetAsync(d_sum, 0, (size_t)nb * sizeof(double), d.stream)) != cudaSuccess ||
-        (e = cudaMemsetAsync(d_sumsq, 0, (size_t)nb * sizeof(double), d.stream)) != cudaSuccess) {
+        (out_bytes && (e = cudaMemsetAsync(d_sum, 0, out_bytes, d.stream)) != cudaSuccess) ||
+        (out_bytes && (e = cudaMemsetAsync(d_sumsq, 0, out_bytes, d.stream)) != cudaSuccess)) {
         p->err = cuda_msg(e, "mc_run_replay_noalloc memset");
         return MC_ERR_CUDA;
     }
@@ -131,8 +136,10 @@ extern "C" mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first, uint64
         return MC_ERR_CUDA;
     }
     if (hs != DS_OK) {
-        p->err = hs == DS_OVERFLOW ? "mc_run_replay_noalloc: more than 16 split copies pending in one history"
-                                   : "mc_run_replay_noalloc: device error status";
+        p->err = hs == DS_OVERFLOW
+                     ? "mc_run_replay_noalloc: more than " + std::to_string(kDepth) +
+                           " particles pending on one history's stack (comb teeth plus split copies)"
+                     : std::string("mc_run_replay_noalloc: ") + device_status_text(hs);
         return status_from_device(hs);
     }
     mc_counters &L = d.last;

@@ -40,6 +40,14 @@ def ce_sphere_small(d, samples=300):
     return d
 
 
+def ce_sphere_bench(d, samples=1000):
+    """The benchmark workload itself (continuous-energy three-shell shield,
+    20,000-point tables for five nuclides, 50-bin lethargy spectrum) at a
+    history count the compiled reference runs in a fraction of a second."""
+    W.ce_sphere(d, samples=samples, n_points=20_000)
+    return d
+
+
 def slab_features(d, samples=400):
     _tables(d, [("700001", 1.0, 6.0, 1e6, 0.3), ("700016", 16.0, 4.0, 3e6, 0.05),
                 ("700012", 12.0, 5.0, 2e6, 0.01)])
@@ -328,6 +336,7 @@ def comb_slab(d, samples=300, bank_max=3, teeth=2):
 # cases the compiled reference can run, with their golden-file names
 REFERENCE_CASES = {
     "ce_sphere_small": ce_sphere_small,
+    "ce_sphere_bench": ce_sphere_bench,
     "slab_features": slab_features,
     "quadrics": quadrics,
     "absorber_slab": absorber_slab,

@@ -7,7 +7,7 @@ uncertainty as C99 hex floats, and a SHA-256 of the per-history event
 digests.  Needs the reference sources, so it runs in the build container
 only; the fixtures it writes are committed and travel everywhere.
 
-    python tests/golden/gen_golden.py [--ref /path/to/MC-old]
+    python tests/golden/gen_golden.py --ref /path/to/MC-old   (or MC_OLD_REF=...)
 """
 import argparse
 import hashlib
@@ -57,8 +57,11 @@ def run_reference(case_dir: str, seed: int):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("MC_OLD_REF"),
+                    help="path of the MC-old checkout (default: $MC_OLD_REF)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref or set MC_OLD_REF to the MC-old checkout")
     build_reference(args.ref)
     for name in cases.REFERENCE_CASES:
         with tempfile.TemporaryDirectory() as d:

@@ -143,16 +143,28 @@ def test_per_thread_stack_overflow_is_a_status(mc):
 
 
 def test_event_overflow_is_a_status(mc):
-    """A tiny overflow bank with heavy splitting reports MC_ERR_OVERFLOW and
-    the handle stays usable."""
+    """The tile kernel's per-CTA overflow bank shrunk to one slot, on a slab
+    whose importance doubles per region (every crossing into a deeper region
+    makes a split copy): MC_ERR_OVERFLOW, and the handle runs again with the
+    default bank, every history once, in agreement with FP64 replay."""
     import mcgpu.workloads as W
+    from stats import assert_agree
     with tempfile.TemporaryDirectory() as d:
         W.mg_deep_slab(d, samples=100, G=4)
         p = mc.Problem(d)
-        p.run(n=5000, mode="event")          # works with the default bank
+        with pytest.raises(mc.McError) as e:
+            p.run(n=20000, mode="event", kernel=1, stack_depth=1)
+        assert e.value.status == 3
+        assert "overflow" in str(e.value)
         p.reset()
-        p.run(n=100, mode="event")
+        c = p.run(n=20000, mode="event", kernel=1)
+        assert c["histories"] == 20000 and c["splits"] > 0
+        m1, s1, _, _ = p.all_tallies()
+        p.reset()
+        p.run(n=20000, first=20000, mode="replay")
+        m2, s2, _, _ = p.all_tallies()
         p.close()
+    assert_agree(m1, s1, m2, s2, "tile kernel after an overflow vs FP64 replay")
 
 
 def test_upload_recopies_the_mixed_engine_tables(mc):

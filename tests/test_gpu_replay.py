@@ -60,13 +60,21 @@ def _extension_cases():
         "mg_deep_slab": lambda d: W.mg_deep_slab(d, samples=400, G=6),
         "mg_layered_slab": lambda d: W.mg_layered_slab(d, samples=600),
         "user_nuclides": lambda d: cases.absorber_slab_user_nuclides(d, samples=500),
+        # the benchmark configurations as written, on a few hundred histories
+        "slab_1g_100_bins": lambda d: W.slab_1g(d, samples=400),
+        "mg_deep_slab_30_groups": lambda d: W.mg_deep_slab(d, samples=400),
+        "mg_layered_slab_detectors": lambda d: W.mg_layered_slab(d, samples=600, detectors=True),
     }
 
 
-@pytest.mark.parametrize("name", ["slab_1g", "mg_deep_slab", "mg_layered_slab", "user_nuclides"])
+@pytest.mark.parametrize("name", ["slab_1g", "mg_deep_slab", "mg_layered_slab", "user_nuclides",
+                                  "slab_1g_100_bins", "mg_deep_slab_30_groups", "mg_layered_slab_detectors"])
 def test_replay_bit_exact_vs_oracle_on_extensions(mc, name):
     """Inputs the reference cannot express (hemisphere source, multigroup
-    data, wr/ws override, capture-only user nuclides): GPU replay = oracle."""
+    data, wr/ws override, capture-only user nuclides): GPU replay = oracle.
+    Among them the 1-group slab with its 100-bin flux, the 30-group
+    deep-penetration slab (importance doubling, wr 0.25 / ws 1) and the
+    16-layer slab, each exactly as benchmarked."""
     with tempfile.TemporaryDirectory() as d:
         _extension_cases()[name](d)
         p = mc.Problem(d, d + "/xs_library")

@@ -57,6 +57,35 @@ def test_noalloc_matches_mc_run_twice(mc, name):
         p.close()
 
 
+def test_noalloc_spans_several_chunks(mc):
+    """A problem with ~5000 tally bins leaves room for ~1090 history rows in
+    the fixed array, so 3000 histories run in three chunks: the chunk loop's
+    reset of the history counter, the reuse of the rows and the ordered fold
+    carrying the sums from one chunk to the next must still give mc_run's
+    replay bit for bit, on two calls in a row."""
+    import torch
+    import mcgpu.workloads as W
+    L = mc.lib()
+    with tempfile.TemporaryDirectory() as d:
+        W.slab_1g(d, samples=10, n_flux_bins=2500)    # 2 x 2500 + 2 bins
+        p = mc.Problem(d, d + "/xs_library")
+        nb = int(sum(p.sizes))
+        assert nb > 5000
+        n, first, seed = 3000, 77, 0x4D43 + 9
+        p.run(n=n, first=first, seed=seed, mode="replay")
+        _, _, s_ref, q_ref = p.all_tallies()
+        out_s = torch.full((nb,), 3.0, dtype=torch.float64, device="cuda")
+        out_q = torch.full((nb,), 3.0, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for call in range(2):
+            st = L.mc_run_replay_noalloc(p._h, first, n, seed, out_s.data_ptr(), out_q.data_ptr())
+            assert st == 0, L.mc_last_error(p._h).decode()
+            assert same_bits(out_s.cpu().numpy(), s_ref), f"call {call + 1}: sums differ from mc_run"
+            assert same_bits(out_q.cpu().numpy(), q_ref), f"call {call + 1}: squares differ from mc_run"
+        assert p.counters()["histories"] == n
+        p.close()
+
+
 def test_noalloc_rejects_too_many_bins(mc):
     """A problem whose tally rows cannot fit the fixed scratch is refused
     with a message, not run."""
