@@ -33,6 +33,7 @@
 #include "orc_philox.h"
 
 #include <float.h>
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -71,9 +72,21 @@ typedef struct {
     size_t n, cap;
 } orc_stack;
 
+/* The reference's per-nuclide grid index (Nuclide::checkE,
+ * Nuclide.cpp:18-24) and per-table last value (XSTable::xs, XSec.cpp:9-40),
+ * kept for the energy they were computed at.  A hit returns the value the
+ * computation would give, so the cache changes no result, only the time. */
+typedef struct {
+    double E_idx;          /* energy of idx (NaN: none yet) */
+    int idx;
+    double E_tab[3];       /* per column (t, s, c) */
+    double xs_tab[3];
+} orc_nuc_cache;
+
 typedef struct {
     const orc_problem *P;
     orc_rng rng;
+    orc_nuc_cache *nc;     /* [n_nuc] */
     double *hist;
     uint64_t *cnt;
     uint64_t digest;
@@ -310,31 +323,42 @@ void orc_surface_reflect(const orc_problem *P, int s, double u[3])
 /* XSec.cpp / Nuclide.cpp / Material.cpp                                     */
 /* ------------------------------------------------------------------------- */
 
-/* XSec.cpp:9-40 with the bin index from Nuclide::checkE (Nuclide.cpp:18-24).
- * The per-table (E, xs) caches of the reference are value-transparent. */
-static double table_xs(const orc_problem *P, int n, const double *col, double E)
+/* XSec.cpp:9-40 with the bin index from Nuclide::checkE (Nuclide.cpp:18-24),
+ * both through the reference's caches (orc_nuc_cache) when c is given. */
+static double table_xs(const orc_problem *P, orc_nuc_cache *c, int n, int k, const double *col, double E)
 {
+    if (c && E == c->E_tab[k]) return c->xs_tab[k];
     const int64_t off = P->nuc_off[n];
     const int len = P->nuc_len[n];
     const double *Eg = P->xs_E + off;
-    const int idx = orc_binary_search(E, Eg, len);
-    if (idx == len - 1) return col[off + len - 1];
-    if (idx == -1) return col[off];
-    return orc_interpolate(E, Eg[idx], Eg[idx + 1], col[off + idx], col[off + idx + 1]);
+    int idx;
+    if (c && E == c->E_idx) {
+        idx = c->idx;
+    } else {
+        idx = orc_binary_search(E, Eg, len);
+        if (c) { c->E_idx = E; c->idx = idx; }
+    }
+    double v;
+    if (idx == len - 1) v = col[off + len - 1];
+    else if (idx == -1) v = col[off];
+    else v = orc_interpolate(E, Eg[idx], Eg[idx + 1], col[off + idx], col[off + idx + 1]);
+    if (c) { c->E_tab[k] = E; c->xs_tab[k] = v; }
+    return v;
 }
 
 enum { XS_T = 0, XS_S, XS_C, XS_A };
 
-static double nuclide_xs(const orc_problem *P, int n, int which, double E)
+static double nuclide_xs(const orc_problem *P, orc_nuc_cache *nc, int n, int which, double E)
 {
     if (P->nuc_kind[n] == ORC_NUC_CONST) {
         /* XSec.cpp:5-7; capture-only nuclide: t = a = c, s = 0 */
         return which == XS_S ? 0.0 : P->nuc_const[n];
     }
+    orc_nuc_cache *c = nc ? nc + n : NULL;
     switch (which) {
-    case XS_T: return table_xs(P, n, P->xs_T, E);
-    case XS_S: return table_xs(P, n, P->xs_S, E);
-    default:   return table_xs(P, n, P->xs_C, E);   /* c and a (= c + f, f = 0) */
+    case XS_T: return table_xs(P, c, n, 0, P->xs_T, E);
+    case XS_S: return table_xs(P, c, n, 1, P->xs_S, E);
+    default:   return table_xs(P, c, n, 2, P->xs_C, E);   /* c and a (= c + f, f = 0) */
     }
 }
 
@@ -353,7 +377,7 @@ static double macro_xs(orc_ctx *C, int m, int which, const orc_particle *p)
     }
     double sum = 0.0;
     for (int i = P->mat_off[m]; i < P->mat_off[m + 1]; ++i)
-        sum += nuclide_xs(P, P->mat_nuc[i], which, p->E) * P->mat_dens[i];
+        sum += nuclide_xs(P, C->nc, P->mat_nuc[i], which, p->E) * P->mat_dens[i];
     return sum;
 }
 
@@ -685,7 +709,7 @@ static void collision(orc_ctx *C, orc_particle *p)
     double s = 0.0;
     int nuc = -1;
     for (int i = P->mat_off[m]; i < P->mat_off[m + 1]; ++i) {
-        s += nuclide_xs(P, P->mat_nuc[i], XS_S, p->E) * P->mat_dens[i];
+        s += nuclide_xs(P, C->nc, P->mat_nuc[i], XS_S, p->E) * P->mat_dens[i];
         if (s > u) { nuc = P->mat_nuc[i]; break; }
     }
     if (nuc < 0) return;
@@ -861,7 +885,13 @@ int orc_run(const orc_problem *P, uint64_t first, uint64_t n, uint64_t seed,
     C.P = P;
     C.cnt = counters;
     C.hist = (double *)calloc((size_t)(nb > 0 ? nb : 1), sizeof(double));
-    if (!C.hist) return ORC_ERR_NOMEM;
+    C.nc = (orc_nuc_cache *)malloc((size_t)(P->n_nuc > 0 ? P->n_nuc : 1) * sizeof(orc_nuc_cache));
+    if (!C.hist || !C.nc) { free(C.hist); free(C.nc); return ORC_ERR_NOMEM; }
+    for (int i = 0; i < P->n_nuc; ++i) {
+        C.nc[i].E_idx = NAN;
+        C.nc[i].idx = 0;
+        for (int k = 0; k < 3; ++k) { C.nc[i].E_tab[k] = NAN; C.nc[i].xs_tab[k] = 0.0; }
+    }
     C.rng.seed = seed;
     for (uint64_t h = 0; h < n && C.status == ORC_OK; ++h) {
         C.rng.history = first + h;
@@ -887,6 +917,7 @@ int orc_run(const orc_problem *P, uint64_t first, uint64_t n, uint64_t seed,
         }
     }
     free(C.hist);
+    free(C.nc);
     free(C.bank.v);
     return C.status;
 }
