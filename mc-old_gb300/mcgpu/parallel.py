@@ -29,16 +29,18 @@ def merge_in_rank_order(parts):
     return s, q
 
 
-def gather_sums(sum_, sumsq, dist, group=None):
+def gather_sums(sum_, sumsq, dist, group=None, device="cpu"):
     """Gather every rank's (sum, sumsq) on all ranks (torch.distributed, any
-    backend) and merge them in rank order."""
+    backend; device "cuda" for NCCL, whose collectives take device tensors)
+    and merge them in rank order."""
     import torch
-    t = torch.from_numpy(np.concatenate([np.asarray(sum_, np.float64), np.asarray(sumsq, np.float64)]))
+    t = torch.from_numpy(np.concatenate([np.asarray(sum_, np.float64),
+                                         np.asarray(sumsq, np.float64)])).to(device)
     world = dist.get_world_size(group)
     outs = [torch.empty_like(t) for _ in range(world)]
     dist.all_gather(outs, t, group=group)
     n = len(sum_)
-    return merge_in_rank_order([(o[:n].numpy(), o[n:].numpy()) for o in outs])
+    return merge_in_rank_order([(o[:n].cpu().numpy(), o[n:].cpu().numpy()) for o in outs])
 
 
 def statistics(sum_, sumsq, n_histories):

@@ -29,9 +29,35 @@ def test_issue_roofline_arithmetic():
     over 4 schedulers per SM x SM clock; absent for shapes without a capture."""
     sys.path.insert(0, ROOT)
     import bench
-    prof = {"issue:k_track:6": 6000.0}
-    r = bench._issue_roofline(prof, {"kernel": 2, "blocks_per_sm": 6}, 1e8, {"sm_mhz": 2000.0}, 150)
+    prof = {"issue:k_track:6": 6000.0, "slab_1g/issue:k_track:8": 100.0}
+    leg = bench.LEGS["ce_sphere"]
+    r = bench._issue_roofline(prof, leg, {"kernel": 2, "blocks_per_sm": 6}, 1e8, {"sm_mhz": 2000.0}, 150)
     assert r["bound"] == "issue" and abs(r["peak"] - 150 * 4 * 2e9) < 1
     assert abs(r["achieved"] - 6e11) < 1 and abs(r["frac"] - 0.5) < 1e-12
-    assert bench._issue_roofline(prof, {"kernel": 2, "blocks_per_sm": 8}, 1e8, {"sm_mhz": 2000.0}, 150) is None
-    assert bench._issue_roofline(prof, {"kernel": 1, "blocks_per_sm": 2}, 1e8, {"sm_mhz": 2000.0}, 150) is None
+    assert bench._issue_roofline(prof, leg, {"kernel": 2, "blocks_per_sm": 8}, 1e8, {"sm_mhz": 2000.0}, 150) is None
+    assert bench._issue_roofline(prof, leg, {"kernel": 1, "blocks_per_sm": 2}, 1e8, {"sm_mhz": 2000.0}, 150) is None
+    r = bench._issue_roofline(prof, bench.LEGS["slab_1g"], {"kernel": 2, "blocks_per_sm": 8}, 1e9,
+                              {"sm_mhz": 2000.0}, 150)
+    assert abs(r["achieved"] - 1e11) < 1
+
+
+def test_algorithmic_bytes_per_workload():
+    """Continuous energy: 16 B per nuclide lookup and per tally update;
+    multigroup: 4 B per cross-section value, 4 B per scatter-CDF probe
+    (ceil(log2 G) per collision), 16 B per tally update."""
+    sys.path.insert(0, ROOT)
+    import bench
+    cnt = {"nuc_lookups": 10, "tally_updates": 3, "xs_evals": 7, "collisions": 2}
+    assert bench._alg_bytes(bench.LEGS["ce_sphere"], cnt) == 16 * 10 + 16 * 3
+    assert bench._alg_bytes(bench.LEGS["mg_deep_slab"], cnt) == 4 * 7 + 4 * 5 * 2 + 16 * 3
+    assert bench._alg_bytes(bench.LEGS["mg_layered_slab"], cnt) == 4 * 7 + 16 * 3
+
+
+def test_reference_arm_runs_every_single_problem_workload():
+    for w in ("slab_1g", "mg_deep_slab", "mg_layered_slab"):
+        r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                            "--warmup", "0", "--ref-histories-per-proc", "50", "--workload", w],
+                           capture_output=True, text=True, timeout=600, cwd=ROOT)
+        assert r.returncode == 0, r.stdout + r.stderr
+        line = json.loads([l for l in r.stdout.splitlines() if l.strip().startswith("{")][0])
+        assert line["impl"] == "reference" and line["value"] > 0 and w in line["config"]["workload"]

@@ -143,14 +143,21 @@ def test_per_thread_stack_overflow_is_a_status(mc):
 
 
 def test_event_overflow_is_a_status(mc):
-    """The tile kernel's per-CTA overflow bank shrunk to one slot, on a slab
-    whose importance doubles per region (every crossing into a deeper region
-    makes a split copy): MC_ERR_OVERFLOW, and the handle runs again with the
-    default bank, every history once, in agreement with FP64 replay."""
+    """The tile kernel's per-CTA overflow bank shrunk to one slot, on a
+    two-region slab whose importance rises 4x at the interface: every
+    crossing into the second region makes three split copies at once, more
+    than the slot holds, so the run stops with MC_ERR_OVERFLOW.  The handle
+    then runs again with the default bank, every history once, in agreement
+    with FP64 replay."""
     import mcgpu.workloads as W
     from stats import assert_agree
     with tempfile.TemporaryDirectory() as d:
-        W.mg_deep_slab(d, samples=100, G=4)
+        tot = np.array([[0.5], [0.5]])
+        sca = np.array([[[0.25]], [[0.25]]])
+        est = ("    <estimator name=\"transmitted\" scores=\"cross\">\n        <surface name=\"p@R\"/>\n"
+               "    </estimator>\n    <estimator name=\"reflected\" scores=\"cross\">\n"
+               "        <surface name=\"p0\"/>\n    </estimator>\n")
+        W._mg_slab_xml(d, "split4", 100, [2.0, 2.0], tot, sca, [1.0, 4.0], est)
         p = mc.Problem(d)
         with pytest.raises(mc.McError) as e:
             p.run(n=20000, mode="event", kernel=1, stack_depth=1)
