@@ -19,8 +19,8 @@ are synthetic, numpy PCG64 seeded, see mcgpu/workloads.py):
   mg_deep_slab     30-group 100 cm deep-penetration slab, importance 2^r,
                    weight roulette 0.25 -> 1; 10^8 histories per step.
   mg_layered_slab  16-layer one-group slab (sigma_t ~ U[0.5, 2]); 10^7
-                   histories per step; with the reflected and interface
-                   currents beside the transmitted one (~5e-9, unresolved).
+                   histories per step; the reflected current beside the
+                   transmitted one (~5e-9, unresolved at this size).
   batch            4096 uneven multigroup shields in one graph launch.
 
 One step = one mc_run over H histories on a fresh history range.  L2 is
@@ -226,11 +226,10 @@ LEGS = {
         "groups": 30, "prof": "mg_deep_slab/",
     },
     "mg_layered_slab": {
-        "desc": "mg_layered_slab: 16 x 1 cm one-group layers, sigma_t ~ U[0.5,2], c ~ U[0.3,0.95], inward plane source",
+        "desc": "mg_layered_slab: 16 x 1 cm one-group layers, sigma_t ~ U[0.5,2], c ~ U[0.3,0.95], inward plane source, transmitted + reflected current",
         "histories": 10_000_000,
         "fom": ("reflected", 0, "reflected current at x = 0"),
-        "more": [("transmitted", 0, "transmitted current at x = 16 cm (~5e-9: unresolved)"),
-                 ("interfaces", 8, "current through the interface at x = 8 cm")],
+        "more": [("transmitted", 0, "transmitted current at x = 16 cm (~5e-9: unresolved)")],
         "groups": 1, "prof": "mg_layered_slab/",
     },
 }
@@ -246,7 +245,7 @@ def make_workload(tmp: str, histories: int, workload: str = "ce_sphere") -> str:
     elif workload == "mg_deep_slab":
         W.mg_deep_slab(d, samples=histories)
     elif workload == "mg_layered_slab":
-        W.mg_layered_slab(d, samples=histories, detectors=True)
+        W.mg_layered_slab(d, samples=histories, detectors="reflected")
     else:
         raise ValueError(workload)
     return d

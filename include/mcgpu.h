@@ -50,12 +50,15 @@ typedef enum {
     /* FP64 history-based with the GPU's native FP64 libm and a tree fold:
      * the plain double-precision GPU history path. */
     MC_FP64_PLAIN = 1,
-    /* FP32 tracking, FP64 tally accumulation.  Two kernels: a persistent
+    /* FP32 tracking, FP64 tally accumulation.  Three engines: a persistent
      * tile of particles per CTA (structure of arrays in shared memory,
-     * ballot/prefix-sum compacted collision and crossing queues), or one
-     * particle per thread in registers; both sample free-gas targets for a
-     * whole warp at once.  mc_tune.kernel or mc_autotune picks one; the
-     * default is the per-thread kernel.  A problem with the particle comb
+     * ballot/prefix-sum compacted collision and crossing queues); one
+     * particle per thread in registers; or the particle bank as a structure
+     * of arrays in HBM with one kernel per event type (advance, collide,
+     * cross) over queues compacted with warp ballots and prefix sums.  All
+     * sample free-gas targets for a whole warp at once and follow the same
+     * tracks.  mc_tune.kernel or mc_autotune picks one; the default is the
+     * per-thread kernel.  A problem with the particle comb
      * (population_control.cpp:55-84) runs on the per-thread kernel, which
      * keeps each history's bank on its thread's stack. */
     MC_MIXED_EVENT = 2
@@ -70,17 +73,25 @@ typedef struct {
                                 per-thread event kernel (0 = 32, or teeth + 32
                                 with the particle comb); the tile kernel: split
                                 copies its CTA's overflow bank holds (0 = 4 per
-                                tile particle) */
+                                tile particle); the event-split engine: split
+                                copies its stack holds (0 = a quarter of the
+                                bank's slots, at least 4096) */
     uint32_t chunk;          /* FP64 modes: histories per fold chunk (0 = auto) */
-    uint32_t bank_capacity;  /* event mode: particles per CTA tile (0 = tuned / 512) */
+    uint32_t bank_capacity;  /* event mode: particles per CTA tile (0 = tuned / 512);
+                                the event-split engine: particle slots of the
+                                HBM bank, a multiple of 256 in 1024..2^24
+                                (0 = 2^20) */
     uint32_t record_digests; /* FP64 modes: keep per-history event digests */
     uint32_t blocks_per_sm;  /* event mode: resident CTAs per SM, which sets the
                                 register budget: 2, 3 or 4 for the tile kernel
                                 (256 threads), 4, 6, 7 or 8 for the per-thread
                                 kernel (128 threads); 0 = tuned / 4 / 8 */
     uint32_t kernel;         /* event mode: 1 = particle tile with event queues,
-                                2 = one particle per thread, 0 = tuned / 2;
-                                the tile kernel refuses the particle comb */
+                                2 = one particle per thread, 3 = event kernels
+                                over an HBM particle bank, 0 = tuned / 2; the
+                                tile kernel and the event-split engine refuse
+                                the particle comb, and batches run kernel 1
+                                or 2 */
     uint32_t max_events;     /* events one particle may take before the run stops
                                 with MC_ERR_TIMEOUT (0 = 2^22); a small cap
                                 exercises that path on purpose */

@@ -48,6 +48,7 @@ SOURCES = [
     ("mc_event_ce.cu", "fast"),
     ("mc_event_mg.cu", "fast"),
     ("mc_event_all.cu", "fast"),
+    ("mc_bank.cu", "fast"),
     ("mc_noalloc.cu", "fp64"),
 ]
 

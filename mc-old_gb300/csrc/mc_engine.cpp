@@ -157,6 +157,8 @@ void device_problem_free(DeviceProblem &d)
     if (d.stream) cudaStreamSynchronize(d.stream);
     event_state_free(d.ev_state);
     d.ev_state = nullptr;
+    bank_state_free(d.bank_state);
+    d.bank_state = nullptr;
     lr_scratch_free(d.lr);
     d.lr = nullptr;
     devbuf_free(d.hist); devbuf_free(d.stack); devbuf_free(d.digest); devbuf_free(d.misc);

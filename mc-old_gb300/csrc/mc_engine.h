@@ -20,6 +20,8 @@ struct DevBuf {
 };
 
 struct EventState;   // mixed-precision event engine (mc_event.cu)
+struct BankState;    // its event-split engine over an HBM particle bank (mc_bank.cu)
+struct EvTables;     // the mixed-precision engine's FP32 tables (mc_evtables.h)
 struct BatchState;   // batches of problems in one persistent launch (mc_event.cu)
 
 struct DeviceProblem {
@@ -42,6 +44,7 @@ struct DeviceProblem {
     DevBuf hist, stack, digest, misc;
     // event engine (owned)
     EventState *ev_state = nullptr;
+    BankState *bank_state = nullptr;   // event-split engine buffers (owned)
     mc_tune tuned{};               // launch shape picked by mc_autotune (0 = defaults)
     void *lr = nullptr;            // forward / backward scratch (mc_lr.cpp)
 };
@@ -65,6 +68,10 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
 mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n, uint64_t seed,
                     const mc_tune *tune, std::string &err);
 void event_state_free(EventState *s);
+// the event-split engine (mc_tune.kernel = 3) on one problem's FP32 tables
+mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t first, uint64_t n, uint64_t seed,
+                   const mc_tune *tune, std::string &err);
+void bank_state_free(BankState *b);
 bool event_tables_ready(const Tables &t, DeviceProblem &d, std::string &err);
 // copies the mixed-precision engine's tables again from pinned host memory
 // (nothing before that engine first ran) and their size in bytes

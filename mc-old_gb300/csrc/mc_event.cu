@@ -171,7 +171,25 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
     L.refill = (tune && tune->refill) ? (int)tune->refill : (tuned.refill ? (int)tuned.refill : refill_default);
     if (L.refill < 1 || L.refill > 32) { err = "refill must be 1..32"; return MC_ERR_ARG; }
     L.kernel = (tune && tune->kernel) ? (int)tune->kernel : (tuned.kernel ? (int)tuned.kernel : 2);
-    if (L.kernel < 1 || L.kernel > 2) { err = "kernel must be 1 (tile) or 2 (per thread)"; return MC_ERR_ARG; }
+    if (L.kernel < 1 || L.kernel > 3) {
+        err = "kernel must be 1 (tile), 2 (per thread) or 3 (event kernels over an HBM bank)";
+        return MC_ERR_ARG;
+    }
+    if (L.kernel == 3 && (batch || comb_teeth > 0)) {
+        // the event-split engine runs one problem and keeps no per-history bank
+        if (tune && tune->kernel) {
+            err = batch ? "the event-split engine (kernel 3) runs single problems, not batches"
+                        : "the particle comb needs a per-history bank: the per-thread kernel (kernel 2) or the FP64 modes";
+            return MC_ERR_ARG;
+        }
+        L.kernel = 2;   // a tuned kernel-3 shape does not apply here
+    }
+    if (L.kernel == 3) {
+        L.block = 256;
+        L.tile = (tune && tune->bank_capacity) ? (int)tune->bank_capacity
+               : ((tuned.kernel == 3 && tuned.bank_capacity) ? (int)tuned.bank_capacity : 0);
+        return MC_OK;   // run_bank sizes the bank and the grids
+    }
     if (comb_teeth > 0 && L.kernel != 2) {
         // the comb acts on one history's bank after each walk; the tile
         // kernel runs a history's particles side by side and has no such bank
@@ -291,6 +309,12 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     const int flavor = (V.has_time || comb) ? FL_ALL : (V.G > 0 ? FL_MG : FL_CE);
     mc_status st = event_launch_shape(d, tune, d.tuned, smem_sums ? nb : 0, false, flavor, comb, L, err);
     if (st != MC_OK) return st;
+    if (L.kernel == 3) {
+        mc_tune bt = tune ? *tune : mc_tune{};
+        bt.bank_capacity = (uint32_t)L.tile;
+        if (!tune) bt.max_events = 0;
+        return run_bank(d, V, flavor, first, n, seed, &bt, err);
+    }
     if ((st = event_scratch(S, d.stream, L.grid, L.tile, L.ovf_cap, nb, err)) != MC_OK) return st;
     char *misc = static_cast<char *>(S.misc.ptr);
     cudaMemsetAsync(misc, 0, 256 + kNumCounters * sizeof(unsigned long long), d.stream);

@@ -65,8 +65,11 @@ enum TileArray {
 //           several bins, through a pair list in local memory) and the
 //           particle comb;
 //   FL_CE   continuous energy, no time filter;
-//   FL_MG   multigroup, no time filter.
-enum Flavor { FL_ALL = 0, FL_CE = 1, FL_MG = 2 };
+//   FL_MG   multigroup, no time filter;
+//   FL_MGB  multigroup, no time filter, every tally through the history row
+//           (the event-split kernels: nothing stays in a thread's registers
+//           from one event kernel to the next).
+enum Flavor { FL_ALL = 0, FL_CE = 1, FL_MG = 2, FL_MGB = 3 };
 
 // 128 threads per CTA lets the register budget step through 128 / 80 / 72 /
 // 64 registers (4 / 6 / 7 / 8 CTAs per SM)
@@ -296,7 +299,7 @@ enum { XT = 0, XS = 1, XC = 2 };
 template <int kFl>
 __device__ __forceinline__ bool is_mg(const EvTables &V)
 {
-    return kFl == FL_MG ? true : (kFl == FL_CE ? false : V.G > 0);
+    return (kFl == FL_MG || kFl == FL_MGB) ? true : (kFl == FL_CE ? false : V.G > 0);
 }
 
 // macroscopic cross section of cell material at the particle's energy/group

@@ -274,13 +274,14 @@ def mg_deep_slab(out_dir: str, samples: int = 100_000_000, n_regions: int = 5, G
 
 
 def mg_layered_slab(out_dir: str, samples: int = 10_000_000, n_regions: int = 16,
-                    tot=None, c=None, detectors: bool = False) -> str:
+                    tot=None, c=None, detectors=False) -> str:
     """16 x 1 cm one-group layered slab (the differentiation workload);
-    transmitted current at the far face.  detectors=True adds the reflected
-    current at x = 0 and the current through every interface (one bin per
-    plane): with sigma_t ~ U[0.5, 2] the slab is ~22 mean free paths thick
-    and its transmission (~5e-9) is far below what 1e7 histories resolve,
-    while these currents are resolved."""
+    transmitted current at the far face.  detectors="reflected" adds the
+    reflected current at x = 0; detectors=True adds it and the current
+    through every interface (one bin per plane).  With sigma_t ~ U[0.5, 2]
+    the slab is ~22 mean free paths thick and its transmission (~5e-9) is
+    far below what 1e7 histories resolve, while these currents are
+    resolved."""
     rng = _rng(5)
     if tot is None:
         tot = rng.uniform(0.5, 2.0, size=n_regions)
@@ -292,7 +293,9 @@ def mg_layered_slab(out_dir: str, samples: int = 10_000_000, n_regions: int = 16
            "    </estimator>\n")
     if detectors:
         est += ("    <estimator name=\"reflected\" scores=\"cross\">\n        <surface name=\"p0\"/>\n"
-                "    </estimator>\n    <estimator name=\"interfaces\" scores=\"cross\">\n"
+                "    </estimator>\n")
+    if detectors is True:
+        est += ("    <estimator name=\"interfaces\" scores=\"cross\">\n"
                 + "".join(f"        <surface name=\"p{i}\"/>\n" for i in range(n_regions + 1))
                 + "    </estimator>\n")
     return _mg_slab_xml(out_dir, "mg_layered_slab", samples, [1.0] * n_regions, tot, sca,

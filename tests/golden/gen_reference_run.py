@@ -12,7 +12,7 @@ mixed-precision tallies with it bin by bin (combined 3 sigma, chi-square).
 Needs the reference sources, so it runs in the build container only; the
 fixture is committed.
 
-    python tests/golden/gen_reference_run.py --ref /path/to/MC-old [--procs 16] [--per-proc 125000]
+    python tests/golden/gen_reference_run.py --ref /path/to/MC-old [--procs 16] [--per-proc 1250000]
 """
 import argparse
 import json
@@ -51,7 +51,7 @@ def main():
     ap.add_argument("--ref", default=os.environ.get("MC_OLD_REF"),
                     help="path of the MC-old checkout (default: $MC_OLD_REF)")
     ap.add_argument("--procs", type=int, default=16)
-    ap.add_argument("--per-proc", type=int, default=125_000)
+    ap.add_argument("--per-proc", type=int, default=1_250_000)
     a = ap.parse_args()
     if not a.ref:
         ap.error("give --ref or set MC_OLD_REF to the MC-old checkout")

