@@ -163,6 +163,34 @@ mc_status mc_reset_tallies(mc_problem *p);
 mc_status mc_state_save(const mc_problem *p, const char *path);
 mc_status mc_state_load(mc_problem *p, const char *path);
 
+/* ---- exact sums: merging disjoint history ranges bit for bit ------------
+ * The reference folds each history into running FP64 sums (sum += h,
+ * squared += h * h, Estimator.cpp:339-346); MC_FP64_REPLAY keeps that order,
+ * so the sums of two runs over [0, a) and [a, n) differ in the last bits from
+ * one run over [0, n) (FP64 addition is not associative).  Alongside, the FP64
+ * modes accumulate every bin's sum of history totals and sum of their squares
+ * exactly, as integers in units of 2^-1074: each value is MC_EXACT_LIMBS
+ * signed 64-bit limbs, value = sum_j limb[j] * 2^(32 j - 1074), normalised
+ * (limbs 0..MC_EXACT_LIMBS-2 in [0, 2^32), the last one signed).  Exact sums
+ * of disjoint ranges (other handles, processes or GPUs) added limb by limb in
+ * any order and rounded once give, bit for bit, the rounded exact sums of one
+ * run over the union: this is the single exchange of a multi-GPU run ("merge
+ * on exact integer accumulators").  No counterpart in the reference, which
+ * runs on one core. */
+#define MC_EXACT_LIMBS 68
+
+/* The exact sums of every bin since the last mc_reset_tallies:
+ * limbs[(b * 2 + k) * MC_EXACT_LIMBS + j], k = 0 sum of history totals,
+ * k = 1 sum of their squares; cap >= n_bins * 2 * MC_EXACT_LIMBS.  Refused
+ * (MC_ERR_ARG) after a mixed-mode or batch run or mc_state_load since that
+ * reset: those add to the FP64 sums only. */
+mc_status mc_exact_sums_read(const mc_problem *p, int64_t *limbs, uint64_t cap);
+
+/* Rounds n_values exact values (MC_EXACT_LIMBS limbs each, normalised or not,
+ * e.g. limb-wise sums over ranks) to the nearest double, ties to even.  Host
+ * arithmetic only. */
+mc_status mc_exact_round(const int64_t *limbs, uint64_t n_values, double *out);
+
 /* Number of estimators (the reference's Estimators.size(), simulator.h:122). */
 mc_status mc_tally_count(const mc_problem *p, uint32_t *n_estimators);
 

@@ -50,6 +50,7 @@ SOURCES = [
     ("mc_event_all.cu", "fast"),
     ("mc_bank.cu", "fast"),
     ("mc_noalloc.cu", "fp64"),
+    ("mc_exact.cu", "fp64"),
 ]
 
 

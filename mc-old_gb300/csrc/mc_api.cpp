@@ -187,6 +187,36 @@ mc_status mc_state_load(mc_problem *p, const char *path)
         return fail(p, MC_ERR_CUDA, cuda_msg(e, "load tallies"));
     d.histories = head[1];
     d.ntrack = head[2];
+    d.exact_valid = false;   // the saved state holds the FP64 sums only
+    return MC_OK;
+}
+
+mc_status mc_exact_sums_read(const mc_problem *p, int64_t *limbs, uint64_t cap)
+{
+    if (!p || !limbs) return MC_ERR_ARG;
+    const DeviceProblem &d = p->dev;
+    const size_t nb = (size_t)std::max<long long>(d.dt.n_bins, 0);
+    const size_t need = nb * 2 * kExactLimbs;
+    if (cap < need)
+        return fail(const_cast<mc_problem *>(p), MC_ERR_ARG,
+                    "mc_exact_sums_read: the buffer holds " + std::to_string(cap) + " limbs, " +
+                        std::to_string(need) + " are needed (n_bins x 2 x MC_EXACT_LIMBS)");
+    if (!d.exact_valid)
+        return fail(const_cast<mc_problem *>(p), MC_ERR_ARG,
+                    "mc_exact_sums_read: a run since the last reset was not an FP64 run (or the tallies "
+                    "were loaded from a saved state), so the exact sums do not cover them");
+    if (need == 0) return MC_OK;
+    cudaError_t e;
+    if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess ||
+        (e = cudaMemcpy(limbs, d.d_exact, need * sizeof(int64_t), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return fail(const_cast<mc_problem *>(p), MC_ERR_CUDA, cuda_msg(e, "read exact sums"));
+    return MC_OK;
+}
+
+mc_status mc_exact_round(const int64_t *limbs, uint64_t n_values, double *out)
+{
+    if ((!limbs || !out) && n_values) return MC_ERR_ARG;
+    for (uint64_t i = 0; i < n_values; ++i) out[i] = exact_round(limbs + i * kExactLimbs);
     return MC_OK;
 }
 

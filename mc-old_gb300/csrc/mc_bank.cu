@@ -612,6 +612,7 @@ mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t fir
     C.launches = launches;
     d.histories += n;
     d.ntrack += C.flights;
+    d.exact_valid = false;   // the mixed mode keeps no per-history rows to sum exactly
     return MC_OK;
 }
 

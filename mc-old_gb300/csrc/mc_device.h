@@ -85,6 +85,18 @@ cudaError_t launch_history_fp64(const DevTables &T, const HistoryArgs &A, bool r
 cudaError_t launch_fold(const double *hist, uint32_t n, long long n_bins, double *sum, double *sq,
                         bool ordered, cudaStream_t st);
 
+// Exact per-bin sums (mc_exact.cu): kExactLimbs signed 64-bit limbs per
+// value, value = sum_j limb[j] * 2^(32 j - 1074); [n_bins][2][kExactLimbs]
+// (sum of history totals, sum of their squares).
+constexpr int kExactLimbs = 68;
+
+// Adds a chunk's per-history totals and their squares to ex exactly.
+cudaError_t launch_fold_exact(const double *hist, uint32_t n, long long n_bins, long long *ex, cudaStream_t st);
+
+// Propagates the carries of every exact value of ex (one representation per
+// value: limbs 0..kExactLimbs-2 in [0, 2^32), the last one signed).
+cudaError_t launch_exact_normalize(long long *ex, long long n_bins, cudaStream_t st);
+
 // Bytes of one FP64 split-stack entry.
 size_t fp64_particle_bytes();
 

@@ -144,7 +144,8 @@ mc_status device_problem_init(const Tables &t, DeviceProblem &d, std::string &er
 
     const size_t nb = (size_t)std::max<int64_t>(t.n_bins(), 1);
     if ((e = cudaMalloc(&d.d_sum, nb * sizeof(double))) != cudaSuccess ||
-        (e = cudaMalloc(&d.d_sq, nb * sizeof(double))) != cudaSuccess) {
+        (e = cudaMalloc(&d.d_sq, nb * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&d.d_exact, nb * 2 * kExactLimbs * sizeof(long long))) != cudaSuccess) {
         err = cuda_msg(e, "cudaMalloc(tallies)");
         return MC_ERR_NOMEM;
     }
@@ -166,6 +167,7 @@ void device_problem_free(DeviceProblem &d)
     if (d.h_blob) cudaFreeHost(d.h_blob);
     if (d.d_sum) cudaFree(d.d_sum);
     if (d.d_sq) cudaFree(d.d_sq);
+    if (d.d_exact) cudaFree(d.d_exact);
     for (auto &ev : d.ev) if (ev) cudaEventDestroy(ev);
     if (d.stream) cudaStreamDestroy(d.stream);
     d = DeviceProblem();
@@ -188,10 +190,12 @@ mc_status reset_tallies(DeviceProblem &d, std::string &err)
     cudaError_t e;
     if ((e = cudaMemsetAsync(d.d_sum, 0, nb * sizeof(double), d.stream)) != cudaSuccess ||
         (e = cudaMemsetAsync(d.d_sq, 0, nb * sizeof(double), d.stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(d.d_exact, 0, nb * 2 * kExactLimbs * sizeof(long long), d.stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(d.stream)) != cudaSuccess) {
         err = cuda_msg(e, "reset tallies");
         return MC_ERR_CUDA;
     }
+    d.exact_valid = true;
     d.histories = 0;
     d.ntrack = 0;
     return MC_OK;
@@ -261,6 +265,9 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
 
     float t_transport = 0.f, t_fold = 0.f;
     uint32_t launches = 0;
+    // the exact sums stay valid only if this run completes
+    const bool exact_was_valid = d.exact_valid;
+    d.exact_valid = false;
     cudaEventRecord(d.ev[0], d.stream);
     for (uint64_t c0 = 0; c0 < n; c0 += chunk) {
         const uint32_t cn = (uint32_t)std::min<uint64_t>(chunk, n - c0);
@@ -283,12 +290,13 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
             return MC_ERR_CUDA;
         }
         cudaEventRecord(d.ev[2], d.stream);
-        if ((e = launch_fold(A.hist, cn, d.dt.n_bins, d.d_sum, d.d_sq, replay, d.stream)) != cudaSuccess) {
+        if ((e = launch_fold(A.hist, cn, d.dt.n_bins, d.d_sum, d.d_sq, replay, d.stream)) != cudaSuccess ||
+            (e = launch_fold_exact(A.hist, cn, d.dt.n_bins, d.d_exact, d.stream)) != cudaSuccess) {
             err = cuda_msg(e, "fold kernel launch");
             return MC_ERR_CUDA;
         }
         cudaEventRecord(d.ev[3], d.stream);
-        launches += 2;
+        launches += 3;
         if (want_digest) {
             cudaMemcpyAsync(d.digests.data() + c0, A.digest, cn * sizeof(uint64_t), cudaMemcpyDeviceToHost, d.stream);
         }
@@ -309,6 +317,11 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
             return status_from_device(hs);
         }
     }
+    if ((e = launch_exact_normalize(d.d_exact, d.dt.n_bins, d.stream)) != cudaSuccess) {
+        err = cuda_msg(e, "exact sums");
+        return MC_ERR_CUDA;
+    }
+    ++launches;
     float total = 0.f;
     cudaEventRecord(d.ev[3], d.stream);
     cudaStreamSynchronize(d.stream);
@@ -329,6 +342,7 @@ mc_status run_fp64(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n
     L.launches = launches;
     d.histories += n;
     d.ntrack += L.flights;
+    d.exact_valid = exact_was_valid;
     return MC_OK;
 }
 

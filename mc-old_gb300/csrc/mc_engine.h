@@ -36,6 +36,8 @@ struct DeviceProblem {
     DevTables dt{};
     double *d_sum = nullptr;       // [n_bins] sum of history totals
     double *d_sq = nullptr;        // [n_bins] sum of squared history totals
+    long long *d_exact = nullptr;  // [n_bins][2][kExactLimbs] exact sums of the FP64 runs
+    bool exact_valid = true;       // every run since the last reset added to d_exact
     uint64_t histories = 0;        // histories folded into d_sum / d_sq
     uint64_t ntrack = 0;           // flights over all runs (the reference's Ntrack)
     mc_counters last{};
@@ -94,6 +96,8 @@ uint64_t batch_problem_seed(uint64_t seed, uint32_t i);
 mc_status status_from_device(int ds);
 // message for a device status word (DS_*) of the FP64 history kernels
 const char *device_status_text(int ds);
+// nearest double (ties to even) of one exact value of kExactLimbs limbs (mc_exact.cu)
+double exact_round(const int64_t *limbs);
 void lr_scratch_free(void *lr);
 std::string cuda_msg(cudaError_t e, const char *what);
 

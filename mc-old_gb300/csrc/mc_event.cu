@@ -367,6 +367,7 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     C.launches = 1;
     d.histories += n;
     d.ntrack += C.flights;
+    d.exact_valid = false;   // the mixed mode keeps no per-history rows to sum exactly
     return MC_OK;
 }
 
@@ -578,7 +579,10 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     b->last.total_ms = ms;
     b->last.launches = 1;
     if (b->count_histories)
-        for (uint32_t i = 0; i < n; ++i) b->probs[i]->histories += b->hist[i];
+        for (uint32_t i = 0; i < n; ++i) {
+            b->probs[i]->histories += b->hist[i];
+            b->probs[i]->exact_valid = false;
+        }
     return MC_OK;
 }
 

@@ -106,6 +106,8 @@ def lib() -> ctypes.CDLL:
         L.mc_batch_last_error.restype = ctypes.c_char_p
         L.mc_last_error.argtypes = [P]
         L.mc_last_error.restype = ctypes.c_char_p
+        L.mc_exact_sums_read.argtypes = [P, P, u64]
+        L.mc_exact_round.argtypes = [P, u64, P]
         L.mc_status_string.argtypes = [st]
         L.mc_status_string.restype = ctypes.c_char_p
         for f in ("mc_problem_load_xml", "mc_problem_free", "mc_problem_upload",
@@ -113,10 +115,25 @@ def lib() -> ctypes.CDLL:
                   "mc_tally_count", "mc_tally_size", "mc_estimator_name", "mc_tally_read",
                   "mc_counters_read", "mc_digests_read", "mc_nsample", "mc_histories_run",
                   "mc_report", "mc_state_save", "mc_state_load", "mc_autotune", "mc_lr_params", "mc_forward", "mc_backward", "mc_backward_density", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
-                  "mc_batch_autotune", "mc_batch_free"):
+                  "mc_batch_autotune", "mc_batch_free", "mc_exact_sums_read", "mc_exact_round"):
             getattr(L, f).restype = st
         _lib = L
     return _lib
+
+
+EXACT_LIMBS = 68   # MC_EXACT_LIMBS
+
+
+def exact_round(limbs) -> np.ndarray:
+    """Nearest doubles of exact values ([..., EXACT_LIMBS] int64 limbs) by the
+    library's mc_exact_round (host arithmetic)."""
+    a = np.ascontiguousarray(limbs, np.int64)
+    n = a.size // EXACT_LIMBS
+    out = np.zeros(max(n, 1))
+    st = lib().mc_exact_round(a.ctypes.data, n, out.ctypes.data)
+    if st != 0:
+        raise McError(st, "mc_exact_round")
+    return out[:n].reshape(a.shape[:-1])
 
 
 def make_tune(**kw) -> Tune:
@@ -210,6 +227,15 @@ class Problem:
         if not parts:
             return (np.zeros(0),) * 4
         return tuple(np.concatenate([p[k] for p in parts]) for k in range(4))
+
+    def exact_sums(self) -> np.ndarray:
+        """Exact per-bin sums of the FP64 runs since the last reset
+        (mc_exact_sums_read): int64 limbs shaped [bins, 2, EXACT_LIMBS]
+        (sum of history totals, sum of their squares)."""
+        nb = int(sum(self.sizes))
+        out = np.zeros((max(nb, 1), 2, EXACT_LIMBS), np.int64)
+        self._check(lib().mc_exact_sums_read(self._h, out.ctypes.data, out.size))
+        return out[:nb]
 
     def digests(self, n: int) -> np.ndarray:
         d = np.zeros(n, np.uint64)

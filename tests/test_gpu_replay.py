@@ -142,3 +142,50 @@ def test_split_stack_overflow_is_a_status(mc):
         p.reset()
         p.run(n=50, mode="replay")        # the handle stays usable
         p.close()
+
+
+def test_exact_sums_match_the_oracle_and_merge_bit_exactly(mc):
+    """The FP64 modes' exact per-bin sums (mc_exact_sums_read): in replay
+    they are the exact sums of the oracle's per-history totals (limb for
+    limb); two handles running disjoint halves merged limb by limb equal the
+    single run; rounded once they equal math.fsum of the history totals, and
+    the running FP64 sums differ from them by rounding only.  After a
+    mixed-mode run the exact sums are refused until the next reset."""
+    import math
+    from mcgpu import parallel
+    from oracle import problem as OP
+    with tempfile.TemporaryDirectory() as d:
+        cases.write_case("slab_features", d)
+        n, a = 600, 233
+        p = mc.Problem(d, d + "/xs_library")
+        p.run(n=n, mode="replay")
+        whole = p.exact_sums()
+        s_run = p.all_tallies()[2]
+        q = mc.Problem(d, d + "/xs_library")
+        q.run(n=a, first=0, mode="replay")
+        h0 = q.exact_sums()
+        q.reset()
+        q.run(n=n - a, first=a, mode="replay")
+        h1 = q.exact_sums()
+        q.reset()
+        q.run(n=n, mode="plain")               # plain FP64 keeps exact sums too
+        plain = q.exact_sums()
+        plain_run = q.all_tallies()[2]
+        q.run(n=100, first=n, mode="event")
+        with pytest.raises(mc.McError) as e:
+            q.exact_sums()
+        assert e.value.status == 8
+        q.reset()
+        assert q.exact_sums().shape == whole.shape
+        q.close()
+        p.close()
+        r = OP.run(OP.load(d, xs_dir=d + "/xs_library"), n=n, hist=True)
+    assert np.array_equal(whole, parallel.exact_limbs_from_values(r.hist))
+    assert np.array_equal(parallel.merge_exact([h1, h0]), whole)
+    rounded = mc.exact_round(whole)
+    assert same_bits(rounded, parallel.round_exact(whole))
+    for b in range(r.hist.shape[1]):
+        assert rounded[b, 0] == math.fsum(r.hist[:, b])
+    assert np.allclose(rounded[:, 0], s_run, rtol=1e-13, atol=1e-300)
+    # plain FP64's tree fold rounds differently from its exact sums, by rounding only
+    assert np.allclose(mc.exact_round(plain)[:, 0], plain_run, rtol=1e-13, atol=1e-300)
