@@ -191,7 +191,8 @@ def _shape(tuned):
     if not tuned:
         return None
     if tuned.get("kernel") == 2:
-        return {"kernel": "per-thread (k_track)", "blocks_per_sm": tuned["blocks_per_sm"]}
+        return {"kernel": "per-thread (k_track)", "blocks_per_sm": tuned["blocks_per_sm"],
+                "refill": tuned.get("refill") or "default"}
     if tuned.get("kernel") == 3:
         return {"kernel": "event kernels over an HBM bank (k_ev_*)", "bank": tuned.get("bank_capacity")}
     return {"kernel": "tile (k_event)", "tile": tuned["bank_capacity"], "blocks_per_sm": tuned["blocks_per_sm"]}

@@ -253,7 +253,8 @@ mc_status mc_run_replay_noalloc(mc_problem *p, uint64_t first_history, uint64_t 
 
 /* Picks the mixed-precision engine's kernel and launch shape (tile kernel:
  * particles per CTA tile and resident CTAs per SM; per-thread kernel:
- * resident CTAs per SM) for this problem by timing sample_histories in each
+ * resident CTAs per SM, then its refill threshold among 2, 4, 8 and 16;
+ * the event-split engine is not sampled) for this problem by timing sample_histories in each
  * candidate shape (at least 4 histories per thread of the largest shape, so
  * that no shape is timed half idle; 0 = 8 per thread); the winner becomes
  * the handle's default for

@@ -53,6 +53,7 @@ mc_status mc_autotune(mc_problem *p, uint64_t sample, uint64_t seed, mc_tune *ou
     double *keep_sum = d.d_sum, *keep_sq = d.d_sq;
     const uint64_t keep_hist = d.histories, keep_ntrack = d.ntrack;
     const mc_counters keep_last = d.last;
+    const bool keep_exact = d.exact_valid;   // the samples go to scratch tallies
     d.d_sum = tmp;
     d.d_sq = tmp + nb;
     std::string err;
@@ -79,12 +80,29 @@ mc_status mc_autotune(mc_problem *p, uint64_t sample, uint64_t seed, mc_tune *ou
             best = t;
         }
     }
+    // the per-thread kernel: how many idle lanes of a warp gather before
+    // they start histories together (short histories favour more)
+    if (st == MC_OK && best.kernel == 2) {
+        const mc_tune shape = best;
+        for (uint32_t r : {2u, 4u, 8u, 16u}) {
+            mc_tune t = shape;
+            t.refill = r;
+            std::string e2;
+            const mc_status s2 = run_event(p->t, d, 0, sample, seed, &t, e2);
+            if (s2 != MC_OK) { st = s2; err = e2; break; }
+            if (d.last.transport_ms < best_ms) {
+                best_ms = (float)d.last.transport_ms;
+                best = t;
+            }
+        }
+    }
     cudaStreamSynchronize(d.stream);
     d.d_sum = keep_sum;
     d.d_sq = keep_sq;
     d.histories = keep_hist;
     d.ntrack = keep_ntrack;
     d.last = keep_last;
+    d.exact_valid = keep_exact;
     cudaFree(tmp);
     if (st != MC_OK) { p->err = "autotune: " + err; return st; }
     if (best.kernel == 0) { p->err = "autotune: no launch shape fits"; return MC_ERR_ARG; }

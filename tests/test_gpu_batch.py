@@ -98,6 +98,7 @@ def test_autotune_single_and_batch(mc):
         t = p.autotune(sample=20000)
         assert t["kernel"] in (1, 2) and t["blocks_per_sm"] in ((2, 3, 4) if t["kernel"] == 1 else (4, 6, 7, 8))
         assert t["kernel"] == 2 or t["bank_capacity"] in (256, 512, 1024, 2048)
+        assert t["kernel"] == 1 or t["refill"] in (0, 2, 4, 8, 16)
         assert np.array_equal(p.all_tallies()[2], before)       # tallies untouched
         assert p.histories_run() == 1000
         p.run(n=1000, first=1000, mode="event")                 # uses the tuned shape
