@@ -6,14 +6,14 @@
 // dies.  Here every live particle of the bank takes one event per iteration,
 // and each iteration is three launches over the bank:
 //
-//   k_bank_advance  the active list plus the empty slots.  An empty slot is
+//   k_bank_advance  every slot of the bank, in slot order.  An empty slot is
 //                   refilled first (a waiting split copy, else a new history
 //                   whose tally row is this slot's own row), then every
 //                   particle takes its flight: cross-section lookup,
 //                   distance to collision and to the cell's surfaces,
 //                   track-length tallies (general.cpp:40-83).  Each particle
 //                   is appended to the collision queue or the crossing
-//                   queue; slots nothing could fill go to the next free list.
+//                   queue.
 //   k_bank_collide  the collision queue: collision tallies, implicit capture,
 //                   scatter nuclide, the free-gas target sampled by the whole
 //                   warp at once, weight roulette (general.cpp:121-163,
@@ -25,13 +25,13 @@
 //                   closes the iteration (swaps the lists, decides whether
 //                   the run is done).
 //
-// Survivors of the collision and crossing kernels are appended to the next
-// iteration's active list, dead particles' slots to its free list.  Every
-// append is one atomic per warp: a ballot gives the lanes that append and
-// their prefix count gives each lane its place.  A particle's state is read
-// and written as 16-byte vectors (position + weight, direction + energy,
-// cell / surface / group / row) at its slot, so a warp's accesses to a run
-// of neighbouring slots coalesce.  The event functions and the random-number
+// A particle stays in its slot from birth to death; a flag per slot says
+// whether it holds one, and a dead particle's slot is refilled by the next
+// advance.  Every queue append is one atomic per warp: a ballot gives the
+// lanes that append and their prefix count gives each lane its place.  A
+// particle's state is read and written as 16-byte vectors (position +
+// weight, direction + energy, cell / surface / group / row) at its slot, so
+// the advance kernel's accesses, in slot order, coalesce.  The event functions and the random-number
 // keying are the other mixed-precision kernels' (mc_event_kernels.cuh), so a
 // particle follows the same track here as in k_track and k_event.
 //
@@ -62,9 +62,7 @@ constexpr int kIterPerCheck = 32;        // iterations between two host checks
 
 struct BankCtl {
     unsigned long long next;     // histories handed out (relative to first)
-    int cur;                     // which active / free list is current
-    int n_act[2];                // particles to advance
-    int n_free[2];               // empty slots
+    int n_live;                  // slots holding a particle
     int n_coll, n_cross;         // this iteration's queues
     int n_split;                 // split copies waiting
     int status;
@@ -82,7 +80,8 @@ struct BankArgs {
     float *t;            // time (problems with a time filter)
     float4 *fx;          // advance -> collide: Sigma_t, Sigma_s, Sigma_c, grid fraction
     int2 *fl;            // advance -> collide / cross: grid index, surface << 2 | (sense + 1)
-    int *act[2], *fre[2], *qc, *qx;
+    int *live;           // [P] the slot holds a particle
+    int *qc, *qx;        // collision / crossing queues (slot indices)
     OvfP *split;         // split copies waiting (a stack)
     int split_cap;
     int P;               // slots
@@ -155,17 +154,16 @@ __device__ __forceinline__ void bank_store(const BankArgs &B, const EvTables &V,
     if (V.has_time) B.t[s] = p.t;
 }
 
-// a dead particle: its slot to the next free list (all lanes call this), its
-// history's row folded when it was the history's last particle
+// a dead particle: its slot empties (all lanes call this, for the count of
+// live slots), its history's row is folded when it was the history's last
+// particle
 template <int kFl>
-__device__ __forceinline__ void bank_retire(Ctx &C, const BankArgs &B, int nxt, bool dies, int s, int hslot,
-                                            bool survives)
+__device__ __forceinline__ void bank_retire(Ctx &C, const BankArgs &B, bool dies, int s, int hslot)
 {
-    const int pa = warp_append(&B.ctl->n_act[nxt], survives);
-    if (survives) B.act[nxt][pa] = s;
-    const int pf = warp_append(&B.ctl->n_free[nxt], dies);
+    const unsigned dm = __ballot_sync(0xffffffffu, dies);
+    if (dm && (threadIdx.x & 31) == __ffs(dm) - 1) atomicSub(&B.ctl->n_live, __popc(dm));
     if (dies) {
-        B.fre[nxt][pf] = s;
+        B.live[s] = 0;
         // the history's other particles may run on other SMs: their tally
         // reductions must be visible before the last one folds the row
         __threadfence();
@@ -180,50 +178,40 @@ template <int kFl>
 __global__ void __launch_bounds__(kBankBlock) k_bank_advance(const EvTables V, const EvArgs A, const BankArgs B)
 {
     __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
-    __shared__ int s_status, s_go;
+    __shared__ int s_status, s_go, s_more;
     const volatile BankCtl *vc = B.ctl;
     if (threadIdx.x == 0) {
         s_status = 0;
         s_go = !(vc->done || vc->status);   // one decision for the whole block
+        s_more = vc->next < A.n;            // histories left to start (it only grows)
     }
     __syncthreads();
     if (!s_go) return;
     Ctx C;
     bank_ctx(C, V, A, s_cnt, &s_status);
-    const int cur = vc->cur, nxt = cur ^ 1;
-    const int na = vc->n_act[cur], nf = vc->n_free[cur];
-    const int total = na + nf;
     const int lane = threadIdx.x & 31;
-    for (int j0 = blockIdx.x * blockDim.x; j0 < total; j0 += gridDim.x * blockDim.x) {
-        const int j = j0 + threadIdx.x;
-        int s = -1;
-        bool live = false, empty = false;
+    for (int s0 = blockIdx.x * blockDim.x; s0 < B.P; s0 += gridDim.x * blockDim.x) {
+        const int s = s0 + threadIdx.x;     // P is a multiple of the block
+        bool live = B.live[s] != 0, fresh = false;
         PState p;
-        if (j < na) {
-            s = B.act[cur][j];
+        if (live) {
             bank_load(B, V, s, p);
-            live = true;
-        } else if (j < total) {
-            s = B.fre[cur][j - na];
-            empty = true;
+        } else if (*(volatile int *)&B.ctl->n_split > 0) {
             // a waiting split copy first (a stack: pops only in this kernel)
-            if (*(volatile int *)&B.ctl->n_split > 0) {
-                const int k = atomicSub(&B.ctl->n_split, 1);
-                if (k > 0) {
-                    const OvfP o = B.split[k - 1];
-                    p.x = o.x; p.y = o.y; p.z = o.z; p.u = o.u; p.v = o.v; p.w = o.w;
-                    p.E = o.E; p.wt = o.wt; p.t = o.t; p.cell = o.cell; p.surf = o.surf;
-                    p.hslot = o.hslot; p.g = o.g; p.id = o.id; p.ev = 0u; p.prob = 0;
-                    live = true;
-                    empty = false;
-                    C.cnt[C_PART]++;
-                } else {
-                    atomicAdd(&B.ctl->n_split, 1);
-                }
+            const int k = atomicSub(&B.ctl->n_split, 1);
+            if (k > 0) {
+                const OvfP o = B.split[k - 1];
+                p.x = o.x; p.y = o.y; p.z = o.z; p.u = o.u; p.v = o.v; p.w = o.w;
+                p.E = o.E; p.wt = o.wt; p.t = o.t; p.cell = o.cell; p.surf = o.surf;
+                p.hslot = o.hslot; p.g = o.g; p.id = o.id; p.ev = 0u; p.prob = 0;
+                fresh = true;
+                C.cnt[C_PART]++;
+            } else {
+                atomicAdd(&B.ctl->n_split, 1);
             }
         }
         // else a new history, in this slot's own row when that row is free
-        const bool want = empty && B.hlive[s] == 0;
+        const bool want = s_more && !live && !fresh && B.hlive[s] == 0;
         const unsigned wm = __ballot_sync(0xffffffffu, want);
         if (wm) {
             const int leader = __ffs(wm) - 1;
@@ -238,15 +226,18 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_advance(const EvTables V, c
                     B.hlive[s] = 1;
                     sample_source(V, A.seed, hist, p);
                     p.hslot = s;
-                    live = true;
-                    empty = false;
+                    fresh = true;
                     C.cnt[C_PART]++;
                 }
             }
         }
-        const int pf = warp_append(&B.ctl->n_free[nxt], empty);
-        if (empty) B.fre[nxt][pf] = s;
-        const bool fresh = live && j >= na;   // placed in the slot just now
+        // slots filled now join the live count (one atomic per warp)
+        const unsigned fm = __ballot_sync(0xffffffffu, fresh);
+        if (fm) {
+            if (lane == __ffs(fm) - 1) atomicAdd(&B.ctl->n_live, __popc(fm));
+            if (fresh) B.live[s] = 1;
+        }
+        live = live || fresh;
         int kind = 0;
         if (live) {
             p.ev += 1u;
@@ -292,7 +283,6 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_collide(const EvTables V, c
     if (!s_go) return;
     Ctx C;
     bank_ctx(C, V, A, s_cnt, &s_status);
-    const int nxt = vc->cur ^ 1;
     const int nc = vc->n_coll;
     // the warp's lanes step through the queue together, so that the
     // free-gas target sampling can share the work across the warp
@@ -333,7 +323,7 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_collide(const EvTables V, c
                 if (is_mg<kFl>(V)) B.meta[s] = make_int4(p.cell, p.surf, p.g, p.hslot);
             }
         }
-        bank_retire<kFl>(C, B, nxt, act && !alive, s, act ? p.hslot : 0, act && alive);
+        bank_retire<kFl>(C, B, act && !alive, s, act ? p.hslot : 0);
     }
     bank_flush(B, s_cnt, s_status);
 }
@@ -352,7 +342,6 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_cross(const EvTables V, con
     if (!s_go) return;
     Ctx C;
     bank_ctx(C, V, A, s_cnt, &s_status);
-    const int cur = vc->cur, nxt = cur ^ 1;
     const int nx = vc->n_cross;
     // split copies wait on the HBM stack; each holds its history open
     auto push = [&](const PState &q, uint32_t cid) -> bool {
@@ -387,7 +376,7 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_cross(const EvTables V, con
             alive = event_cross<kFl>(C, V, R, p, f, push);
             if (alive) bank_store(B, V, s, p);
         }
-        bank_retire<kFl>(C, B, nxt, act && !alive, s, act ? p.hslot : 0, act && alive);
+        bank_retire<kFl>(C, B, act && !alive, s, act ? p.hslot : 0);
     }
     bank_flush(B, s_cnt, s_status);
     // the last block to finish closes the iteration
@@ -397,13 +386,10 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_cross(const EvTables V, con
         if (t == gridDim.x - 1) {
             __threadfence();
             volatile BankCtl *c = B.ctl;
-            c->n_act[cur] = 0;
-            c->n_free[cur] = 0;
             c->n_coll = 0;
             c->n_cross = 0;
-            c->cur = nxt;
             c->iter = c->iter + 1u;
-            if (c->n_act[nxt] == 0 && c->n_split <= 0 && c->next >= A.n) c->done = 1;
+            if (c->n_live == 0 && c->n_split <= 0 && c->next >= A.n) c->done = 1;
             c->blocks_done = 0u;
             __threadfence();
         }
@@ -413,12 +399,11 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_cross(const EvTables V, con
 __global__ void k_bank_init(BankArgs B)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.P; i += gridDim.x * blockDim.x) {
-        B.fre[0][i] = i;
+        B.live[i] = 0;
         B.hlive[i] = 0;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         BankCtl c{};
-        c.n_free[0] = B.P;
         *B.ctl = c;
     }
 }
@@ -491,7 +476,7 @@ mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t fir
     // one allocation for the bank's arrays, 256-byte aligned sections
     const size_t Pz = (size_t)P;
     const size_t sizes[] = {16 * Pz, 16 * Pz, 16 * Pz, 8 * Pz, 4 * Pz, 16 * Pz, 8 * Pz,
-                            4 * Pz, 4 * Pz, 4 * Pz, 4 * Pz, 4 * Pz, 4 * Pz, 8 * Pz, 4 * Pz};
+                            4 * Pz, 4 * Pz, 4 * Pz, 8 * Pz, 4 * Pz};
     size_t total = 0;
     for (size_t z : sizes) total += (z + 255) & ~(size_t)255;
     const size_t row_bytes = Pz * (size_t)nb * sizeof(double);
@@ -521,14 +506,11 @@ mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t fir
     B.t = reinterpret_cast<float *>(take(sizes[4]));
     B.fx = reinterpret_cast<float4 *>(take(sizes[5]));
     B.fl = reinterpret_cast<int2 *>(take(sizes[6]));
-    B.act[0] = reinterpret_cast<int *>(take(sizes[7]));
-    B.act[1] = reinterpret_cast<int *>(take(sizes[8]));
-    B.fre[0] = reinterpret_cast<int *>(take(sizes[9]));
-    B.fre[1] = reinterpret_cast<int *>(take(sizes[10]));
-    B.qc = reinterpret_cast<int *>(take(sizes[11]));
-    B.qx = reinterpret_cast<int *>(take(sizes[12]));
-    B.hidx = reinterpret_cast<unsigned long long *>(take(sizes[13]));
-    B.hlive = reinterpret_cast<int *>(take(sizes[14]));
+    B.live = reinterpret_cast<int *>(take(sizes[7]));
+    B.qc = reinterpret_cast<int *>(take(sizes[8]));
+    B.qx = reinterpret_cast<int *>(take(sizes[9]));
+    B.hidx = reinterpret_cast<unsigned long long *>(take(sizes[10]));
+    B.hlive = reinterpret_cast<int *>(take(sizes[11]));
     B.split = static_cast<OvfP *>(S.split.ptr);
     B.split_cap = split_cap;
     B.P = P;
