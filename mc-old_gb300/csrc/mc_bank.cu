@@ -89,15 +89,19 @@ struct BankArgs {
     int *hlive;                 // [P] the row's history: particles alive or waiting
     BankCtl *ctl;
     unsigned long long *bcnt;   // [grid][kNumCounters] per-block event counters
+    int may_split;              // cells differ in importance: a history may own several particles
 };
 
-__device__ __forceinline__ void bank_ctx(Ctx &C, const EvTables &V, const EvArgs &A, uint32_t *s_cnt, int *s_status)
+// sums: the block's shared tally sums (2 x n_bins doubles; nullptr = the
+// global sums take each history's fold directly)
+__device__ __forceinline__ void bank_ctx(Ctx &C, const EvTables &V, const EvArgs &A, uint32_t *s_cnt, int *s_status,
+                                         double *sums = nullptr)
 {
     C.V = &V;
     C.A = &A;
-    C.T.base = nullptr;
+    C.T.base = reinterpret_cast<unsigned char *>(sums);
     C.T.P = 0;
-    C.T.nsum = 0;
+    C.T.nsum = sums ? V.n_bins : 0;
     C.s_status = s_status;
     C.s_novf = nullptr;
     C.s_nlive = nullptr;
@@ -113,9 +117,17 @@ __device__ __forceinline__ void bank_ctx(Ctx &C, const EvTables &V, const EvArgs
 
 // The block's event counters into its own slot of the per-block array (one
 // block of a launch per slot: plain adds, no contention), and its status.
-__device__ __forceinline__ void bank_flush(const BankArgs &B, uint32_t *s_cnt, int s_status)
+__device__ __forceinline__ void bank_flush(const BankArgs &B, uint32_t *s_cnt, int s_status,
+                                           const EvArgs *A = nullptr, const double *sums = nullptr, long long nb = 0)
 {
     __syncthreads();
+    if (sums) {   // the block's folded histories, one global atomic per nonzero bin
+        for (long long b = threadIdx.x; b < nb; b += blockDim.x) {
+            const double sv = sums[b], qv = sums[nb + b];
+            if (sv != 0.0) atomicAdd(A->sum + b, sv);
+            if (qv != 0.0) atomicAdd(A->sq + b, qv);
+        }
+    }
     __shared__ unsigned long long s_red[kBankBlock / 32][kNumCounters];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = 0; i < kNumCounters; ++i) {
@@ -164,11 +176,13 @@ __device__ __forceinline__ void bank_retire(Ctx &C, const BankArgs &B, bool dies
     if (dm && (threadIdx.x & 31) == __ffs(dm) - 1) atomicSub(&B.ctl->n_live, __popc(dm));
     if (dies) {
         B.live[s] = 0;
-        // the history's other particles may run on other SMs: their tally
-        // reductions must be visible before the last one folds the row
-        __threadfence();
+        // with splitting, the history's other particles may run on other
+        // SMs in this same kernel: their tally reductions must be visible
+        // before the last one folds the row.  Without it the history's one
+        // particle made every reduction itself, in this or an earlier kernel.
+        if (B.may_split) __threadfence();
         if (atomicSub(&B.hlive[hslot], 1) == 1) {
-            __threadfence();
+            if (B.may_split) __threadfence();
             history_fold<kFl, false>(C, hslot, 0);
         }
     }
@@ -282,7 +296,14 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_collide(const EvTables V, c
     __syncthreads();
     if (!s_go) return;
     Ctx C;
-    bank_ctx(C, V, A, s_cnt, &s_status);
+    // histories that end here fold into the block's shared sums first
+    extern __shared__ double s_sums[];
+    double *sums = A.smem_sums ? s_sums : nullptr;
+    if (sums) {
+        for (long long b = threadIdx.x; b < 2 * V.n_bins; b += blockDim.x) sums[b] = 0.0;
+        __syncthreads();
+    }
+    bank_ctx(C, V, A, s_cnt, &s_status, sums);
     const int nc = vc->n_coll;
     // the warp's lanes step through the queue together, so that the
     // free-gas target sampling can share the work across the warp
@@ -325,7 +346,7 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_collide(const EvTables V, c
         }
         bank_retire<kFl>(C, B, act && !alive, s, act ? p.hslot : 0);
     }
-    bank_flush(B, s_cnt, s_status);
+    bank_flush(B, s_cnt, s_status, &A, sums, V.n_bins);
 }
 
 template <int kFl>
@@ -341,7 +362,14 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_cross(const EvTables V, con
     __syncthreads();
     if (!s_go) return;
     Ctx C;
-    bank_ctx(C, V, A, s_cnt, &s_status);
+    // histories that end here fold into the block's shared sums first
+    extern __shared__ double s_sums[];
+    double *sums = A.smem_sums ? s_sums : nullptr;
+    if (sums) {
+        for (long long b = threadIdx.x; b < 2 * V.n_bins; b += blockDim.x) sums[b] = 0.0;
+        __syncthreads();
+    }
+    bank_ctx(C, V, A, s_cnt, &s_status, sums);
     const int nx = vc->n_cross;
     // split copies wait on the HBM stack; each holds its history open
     auto push = [&](const PState &q, uint32_t cid) -> bool {
@@ -378,7 +406,7 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_cross(const EvTables V, con
         }
         bank_retire<kFl>(C, B, act && !alive, s, act ? p.hslot : 0);
     }
-    bank_flush(B, s_cnt, s_status);
+    bank_flush(B, s_cnt, s_status, &A, sums, V.n_bins);
     // the last block to finish closes the iteration
     if (threadIdx.x == 0) {
         __threadfence();
@@ -443,8 +471,8 @@ void bank_state_free(BankState *b)
     delete b;
 }
 
-mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t first, uint64_t n, uint64_t seed,
-                   const mc_tune *tune, std::string &err)
+mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, bool may_split, uint64_t first, uint64_t n,
+                   uint64_t seed, const mc_tune *tune, std::string &err)
 {
     if (!d.bank_state) d.bank_state = new BankState();
     BankState &S = *d.bank_state;
@@ -458,8 +486,9 @@ mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t fir
     const BankKernels K = bank_kernels(flavor);
     int per_sm = 0, per_sm_c = 0, per_sm_x = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, K.adv, kBankBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, K.col, kBankBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_x, K.crs, kBankBlock, 0);
+    const size_t occ_smem = (V.n_bins > 0 && V.n_bins <= 1024) ? 2 * (size_t)V.n_bins * sizeof(double) : 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, K.col, kBankBlock, occ_smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_x, K.crs, kBankBlock, occ_smem);
     if (per_sm < 1 || per_sm_c < 1 || per_sm_x < 1) { err = "event-split kernels do not fit on an SM"; return MC_ERR_CUDA; }
     const int grid_a = (tune && tune->grid_blocks) ? (int)tune->grid_blocks : d.sms * per_sm;
     const int grid_c = (tune && tune->grid_blocks) ? (int)tune->grid_blocks : d.sms * per_sm_c;
@@ -516,6 +545,7 @@ mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t fir
     B.P = P;
     B.ctl = static_cast<BankCtl *>(S.ctl.ptr);
     B.bcnt = static_cast<unsigned long long *>(S.bcnt.ptr);
+    B.may_split = may_split ? 1 : 0;
 
     EvArgs A{};
     A.first = first;
@@ -529,7 +559,12 @@ mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t fir
     A.sum = d.d_sum;
     A.sq = d.d_sq;
     A.tile = 0;          // tally row = the history's slot
-    A.smem_sums = 0;
+    // the collide and cross kernels fold ending histories into per-block
+    // shared sums (one global atomic per nonzero bin and block) when the
+    // problem has at most 1024 bins; else straight into the global sums
+    const bool smem_sums = V.n_bins > 0 && V.n_bins <= 1024;
+    const size_t sum_smem = smem_sums ? 2 * (size_t)V.n_bins * sizeof(double) : 0;
+    A.smem_sums = smem_sums ? 1 : 0;
     A.n_prob = 0;
 
     cudaError_t e;
@@ -546,8 +581,8 @@ mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t fir
     for (;;) {
         for (int k = 0; k < kIterPerCheck; ++k) {
             K.adv<<<grid_a, kBankBlock, 0, d.stream>>>(V, A, B);
-            K.col<<<grid_c, kBankBlock, 0, d.stream>>>(V, A, B);
-            K.crs<<<grid_x, kBankBlock, 0, d.stream>>>(V, A, B);
+            K.col<<<grid_c, kBankBlock, sum_smem, d.stream>>>(V, A, B);
+            K.crs<<<grid_x, kBankBlock, sum_smem, d.stream>>>(V, A, B);
         }
         launches += 3 * kIterPerCheck;
         iters += kIterPerCheck;

@@ -71,8 +71,9 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
                     const mc_tune *tune, std::string &err);
 void event_state_free(EventState *s);
 // the event-split engine (mc_tune.kernel = 3) on one problem's FP32 tables
-mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, uint64_t first, uint64_t n, uint64_t seed,
-                   const mc_tune *tune, std::string &err);
+// may_split: cells differ in importance, so a history can own several particles
+mc_status run_bank(DeviceProblem &d, const EvTables &V, int flavor, bool may_split, uint64_t first, uint64_t n,
+                   uint64_t seed, const mc_tune *tune, std::string &err);
 void bank_state_free(BankState *b);
 bool event_tables_ready(const Tables &t, DeviceProblem &d, std::string &err);
 // copies the mixed-precision engine's tables again from pinned host memory

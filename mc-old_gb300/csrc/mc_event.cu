@@ -313,7 +313,15 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
         mc_tune bt = tune ? *tune : mc_tune{};
         bt.bank_capacity = (uint32_t)L.tile;
         if (!tune) bt.max_events = 0;
-        return run_bank(d, V, flavor, first, n, seed, &bt, err);
+        // importance splitting needs two cells of different nonzero importance
+        bool may_split = false;
+        double imp0 = 0.0;
+        for (double imp : t.cell_imp) {
+            if (imp <= 0.0) continue;
+            if (imp0 == 0.0) imp0 = imp;
+            else if (imp != imp0) may_split = true;
+        }
+        return run_bank(d, V, flavor, may_split, first, n, seed, &bt, err);
     }
     if ((st = event_scratch(S, d.stream, L.grid, L.tile, L.ovf_cap, nb, err)) != MC_OK) return st;
     char *misc = static_cast<char *>(S.misc.ptr);
