@@ -22,8 +22,8 @@
 //                   crossing tallies, importance roulette / splitting
 //                   (general.cpp:89-115, population_control.cpp:21-49); split
 //                   copies wait in an HBM stack.  The last block to finish
-//                   closes the iteration (swaps the lists, decides whether
-//                   the run is done).
+//                   closes the iteration (empties the queues, decides
+//                   whether the run is done).
 //
 // A particle stays in its slot from birth to death; a flag per slot says
 // whether it holds one, and a dead particle's slot is refilled by the next
@@ -31,9 +31,10 @@
 // lanes that append and their prefix count gives each lane its place.  A
 // particle's state is read and written as 16-byte vectors (position +
 // weight, direction + energy, cell / surface / group / row) at its slot, so
-// the advance kernel's accesses, in slot order, coalesce.  The event functions and the random-number
-// keying are the other mixed-precision kernels' (mc_event_kernels.cuh), so a
-// particle follows the same track here as in k_track and k_event.
+// the advance kernel's accesses, in slot order, coalesce.  The event
+// functions and the random-number keying are the other mixed-precision
+// kernels' (mc_event_kernels.cuh), so a particle follows the same track here
+// as in k_track and k_event.
 //
 // Tallies: a history's tallies go to the tally row of the slot that started
 // it, as reductions in L2; when its last particle dies the row's touched bins
