@@ -650,7 +650,8 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
                 err = float(np.sqrt(np.sum(s ** 2))) / tot
                 foms.append(1.0 / (err * err * T))
         # e2e through the C ABI: every problem's tables uploaded again from
-        # pinned host memory, the batch run, every problem's tallies read back
+        # pinned host memory, the tallies cleared, the batch run, every
+        # problem's tallies read back (the batch-wide calls: one wait each)
         e2e_t = 0.0
         h2d = int(sum(p.table_bytes() for p in probs))
         d2h = 0
@@ -658,15 +659,12 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
             flush.zero_()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            for p in probs:
-                p.upload()
-                p.reset()
+            b.upload()
+            b.reset()
             b.run(seed=SEED + 100 + k, **run_kw)
-            d2h = 0
-            for p in probs:
-                tot = p.all_tallies()
-                d2h += int(sum(x.nbytes for x in tot[2:]))
+            tot = b.tallies()
             e2e_t += time.perf_counter() - t0
+            d2h = int(sum(x.nbytes for x in tot[2:]))
         b.close()
         for p in probs:
             p.close()

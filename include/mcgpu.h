@@ -318,6 +318,18 @@ mc_status mc_batch_counters(const mc_batch *b, mc_counters *out);
  * per-thread kernel's refill threshold among 2, 4, 8 and 16, and keeps the
  * fastest for runs with tune == NULL; the problems' tallies are untouched. */
 mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double sample_fraction, mc_tune *out);
+/* Batch-wide forms of mc_problem_upload, mc_reset_tallies and mc_tally_read,
+ * for callers that move every problem's tables and tallies at each run: the
+ * copies and clears of all problems are queued on the batch's stream and
+ * waited for once, instead of once per problem.  mc_batch_tally_read writes
+ * every problem's bins (all its estimators in order), problem after problem,
+ * into each non-NULL array of cap >= the batch's total bins, with the
+ * statistics of mc_tally_read over each problem's own histories.  Each call
+ * first waits for every problem's own stream.  No counterpart in the
+ * reference. */
+mc_status mc_batch_upload(mc_batch *b);
+mc_status mc_batch_reset(mc_batch *b);
+mc_status mc_batch_tally_read(mc_batch *b, double *mean, double *sigma, double *sum, double *sumsq, uint64_t cap);
 mc_status mc_batch_free(mc_batch *b);
 const char *mc_batch_last_error(const mc_batch *b);
 

@@ -18,6 +18,8 @@ struct mc_batch {
     mc_tune tuned{};
     int sms = 0;
     std::string err;
+    double *h_stage = nullptr;   // pinned: every problem's sums, read back in one pass
+    size_t stage_doubles = 0;
 };
 
 namespace {
@@ -226,10 +228,113 @@ mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double frac, mc_tune *ou
     return MC_OK;
 }
 
+// Every problem's own stream first: a problem must not still be working on
+// its own when the batch stream touches its tables or sums.
+static mc_status batch_quiesce(mc_batch *b)
+{
+    for (mc_problem *p : b->probs) {
+        const cudaError_t e = cudaStreamSynchronize(p->dev.stream);
+        if (e != cudaSuccess) { b->err = cuda_msg(e, "problem stream"); return MC_ERR_CUDA; }
+    }
+    return MC_OK;
+}
+
+mc_status mc_batch_upload(mc_batch *b)
+{
+    if (!b || !b->state) return MC_ERR_ARG;
+    mc_status st = batch_quiesce(b);
+    if (st != MC_OK) return st;
+    const cudaStream_t s = batch_stream(b->state);
+    cudaError_t e = cudaSuccess;
+    for (mc_problem *p : b->probs) {
+        if ((e = upload_tables_async(p->dev, s)) != cudaSuccess ||
+            (e = event_tables_upload_async(p->dev, s)) != cudaSuccess)
+            break;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { b->err = cuda_msg(e, "batch upload"); return MC_ERR_CUDA; }
+    return MC_OK;
+}
+
+mc_status mc_batch_reset(mc_batch *b)
+{
+    if (!b || !b->state) return MC_ERR_ARG;
+    mc_status st = batch_quiesce(b);
+    if (st != MC_OK) return st;
+    const cudaStream_t s = batch_stream(b->state);
+    cudaError_t e = cudaSuccess;
+    for (mc_problem *p : b->probs)
+        if ((e = reset_tallies_async(p->dev, s)) != cudaSuccess) break;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { b->err = cuda_msg(e, "batch reset"); return MC_ERR_CUDA; }
+    return MC_OK;
+}
+
+mc_status mc_batch_tally_read(mc_batch *b, double *mean, double *sigma, double *sum, double *sumsq,
+                              uint64_t cap)
+{
+    if (!b || !b->state) return MC_ERR_ARG;
+    uint64_t total = 0;
+    for (mc_problem *p : b->probs) total += (uint64_t)std::max<long long>(p->dev.dt.n_bins, 0);
+    if (cap < total && (mean || sigma || sum || sumsq)) {
+        b->err = "mc_batch_tally_read: the arrays hold " + std::to_string(cap) + " bins, the batch has " +
+                 std::to_string(total);
+        return MC_ERR_ARG;
+    }
+    mc_status st = batch_quiesce(b);
+    if (st != MC_OK) return st;
+    if (b->stage_doubles < 2 * total) {
+        if (b->h_stage) cudaFreeHost(b->h_stage);
+        b->h_stage = nullptr;
+        b->stage_doubles = 0;
+        if (cudaHostAlloc(&b->h_stage, std::max<size_t>(2 * total, 1) * sizeof(double), cudaHostAllocDefault) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            b->err = "cannot allocate the batch's read-back buffer";
+            return MC_ERR_NOMEM;
+        }
+        b->stage_doubles = 2 * total;
+    }
+    const cudaStream_t s = batch_stream(b->state);
+    cudaError_t e = cudaSuccess;
+    uint64_t off = 0;
+    for (mc_problem *p : b->probs) {
+        const size_t nb = (size_t)std::max<long long>(p->dev.dt.n_bins, 0);
+        if (nb == 0) continue;
+        if ((e = cudaMemcpyAsync(b->h_stage + off, p->dev.d_sum, nb * sizeof(double), cudaMemcpyDeviceToHost, s)) !=
+                cudaSuccess ||
+            (e = cudaMemcpyAsync(b->h_stage + total + off, p->dev.d_sq, nb * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            break;
+        off += nb;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { b->err = cuda_msg(e, "batch tally read"); return MC_ERR_CUDA; }
+    // per problem, the statistics of mc_tally_read (Estimator.cpp:347-367)
+    // over that problem's histories
+    off = 0;
+    for (mc_problem *p : b->probs) {
+        const uint64_t nb = (uint64_t)std::max<long long>(p->dev.dt.n_bins, 0);
+        const double N = (double)p->dev.histories;
+        for (uint64_t j = 0; j < nb; ++j) {
+            const double sv = b->h_stage[off + j], qv = b->h_stage[total + off + j];
+            const double m = sv / N;
+            const double us = (qv / N - m * m) / (N - 1.0);
+            if (mean) mean[off + j] = (0.0 + m) / 1.0;
+            if (sigma) sigma[off + j] = std::sqrt(0.0 + us) / 1.0;
+            if (sum) sum[off + j] = sv;
+            if (sumsq) sumsq[off + j] = qv;
+        }
+        off += nb;
+    }
+    return MC_OK;
+}
+
 mc_status mc_batch_free(mc_batch *b)
 {
     if (!b) return MC_ERR_ARG;
     batch_state_free(b->state);
+    if (b->h_stage) cudaFreeHost(b->h_stage);
     delete b;
     return MC_OK;
 }

@@ -184,6 +184,25 @@ mc_status upload_tables(DeviceProblem &d, std::string &err)
     return MC_OK;
 }
 
+cudaError_t upload_tables_async(DeviceProblem &d, cudaStream_t st)
+{
+    return cudaMemcpyAsync(d.blob, d.h_blob, d.blob_bytes, cudaMemcpyHostToDevice, st);
+}
+
+cudaError_t reset_tallies_async(DeviceProblem &d, cudaStream_t st)
+{
+    const size_t nb = (size_t)std::max<long long>(d.dt.n_bins, 1);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(d.d_sum, 0, nb * sizeof(double), st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(d.d_sq, 0, nb * sizeof(double), st)) != cudaSuccess ||
+        (e = cudaMemsetAsync(d.d_exact, 0, nb * 2 * kExactLimbs * sizeof(long long), st)) != cudaSuccess)
+        return e;
+    d.exact_valid = true;
+    d.histories = 0;
+    d.ntrack = 0;
+    return cudaSuccess;
+}
+
 mc_status reset_tallies(DeviceProblem &d, std::string &err)
 {
     const size_t nb = (size_t)std::max<long long>(d.dt.n_bins, 1);

@@ -55,6 +55,10 @@ mc_status device_problem_init(const Tables &t, DeviceProblem &d, std::string &er
 void device_problem_free(DeviceProblem &d);
 mc_status reset_tallies(DeviceProblem &d, std::string &err);
 mc_status upload_tables(DeviceProblem &d, std::string &err);
+// the same on a caller's stream, without waiting (batches queue many problems)
+cudaError_t upload_tables_async(DeviceProblem &d, cudaStream_t st);
+cudaError_t reset_tallies_async(DeviceProblem &d, cudaStream_t st);
+cudaError_t event_tables_upload_async(DeviceProblem &d, cudaStream_t st);
 mc_status read_sums(const DeviceProblem &d, std::vector<double> &sum, std::vector<double> &sq, std::string &err);
 mc_status run_histories(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n, uint64_t seed,
                         mc_mode mode, const mc_tune *tune, std::string &err);

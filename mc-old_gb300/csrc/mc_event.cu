@@ -145,6 +145,13 @@ mc_status event_tables_upload(DeviceProblem &d, std::string &err)
     return MC_OK;
 }
 
+cudaError_t event_tables_upload_async(DeviceProblem &d, cudaStream_t st)
+{
+    if (!d.ev_state) return cudaSuccess;   // the mixed-precision engine has not run yet
+    const EventState &S = *d.ev_state;
+    return cudaMemcpyAsync(S.d_blob, S.h_blob, S.blob_bytes, cudaMemcpyHostToDevice, st);
+}
+
 size_t event_table_bytes(const DeviceProblem &d) { return d.ev_state ? d.ev_state->blob_bytes : 0; }
 
 const EvTables &event_tables_view(const DeviceProblem &d) { return d.ev_state->dv; }

@@ -102,6 +102,9 @@ def lib() -> ctypes.CDLL:
         L.mc_batch_counters.argtypes = [P, ctypes.POINTER(Counters)]
         L.mc_batch_autotune.argtypes = [P, u64, ctypes.c_double, ctypes.POINTER(Tune)]
         L.mc_batch_free.argtypes = [P]
+        L.mc_batch_upload.argtypes = [P]
+        L.mc_batch_reset.argtypes = [P]
+        L.mc_batch_tally_read.argtypes = [P, P, P, P, P, u64]
         L.mc_batch_last_error.argtypes = [P]
         L.mc_batch_last_error.restype = ctypes.c_char_p
         L.mc_last_error.argtypes = [P]
@@ -115,7 +118,8 @@ def lib() -> ctypes.CDLL:
                   "mc_tally_count", "mc_tally_size", "mc_estimator_name", "mc_tally_read",
                   "mc_counters_read", "mc_digests_read", "mc_nsample", "mc_histories_run",
                   "mc_report", "mc_state_save", "mc_state_load", "mc_autotune", "mc_lr_params", "mc_forward", "mc_backward", "mc_backward_density", "mc_batch_create", "mc_batch_run", "mc_batch_counters",
-                  "mc_batch_autotune", "mc_batch_free", "mc_exact_sums_read", "mc_exact_round"):
+                  "mc_batch_autotune", "mc_batch_free", "mc_exact_sums_read", "mc_exact_round",
+                  "mc_batch_upload", "mc_batch_reset", "mc_batch_tally_read"):
             getattr(L, f).restype = st
         _lib = L
     return _lib
@@ -354,6 +358,22 @@ class Batch:
         t = Tune()
         self._check(lib().mc_batch_autotune(self._h, seed, fraction, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def upload(self):
+        """Every problem's tables again from pinned host memory, one wait."""
+        self._check(lib().mc_batch_upload(self._h))
+
+    def reset(self):
+        """Every problem's tallies zeroed, one wait."""
+        self._check(lib().mc_batch_reset(self._h))
+
+    def tallies(self):
+        """(mean, sigma, sum, sumsq) of every problem's bins, problem after
+        problem, in one read-back (mc_batch_tally_read)."""
+        total = int(sum(sum(p.sizes) for p in self.problems))
+        out = [np.zeros(max(total, 1)) for _ in range(4)]
+        self._check(lib().mc_batch_tally_read(self._h, *[a.ctypes.data for a in out], max(total, 1)))
+        return tuple(a[:total] for a in out)
 
     def close(self):
         if getattr(self, "_h", None):

@@ -116,3 +116,30 @@ def test_autotune_single_and_batch(mc):
         b.close()
         for p in probs:
             p.close()
+
+
+def test_batch_wide_upload_reset_and_read(mc):
+    """mc_batch_upload / mc_batch_reset / mc_batch_tally_read do for every
+    problem what the per-problem calls do, with one wait each: the batch's
+    read-back equals every problem's own mc_tally_read bit for bit, a reset
+    zeroes every problem, and after a batch upload the same seed gives the
+    same tallies again."""
+    with tempfile.TemporaryDirectory() as root:
+        probs, hist = _problems(mc, root, 16)
+        b = mc.Batch(probs, hist)
+        b.run(seed=5)
+        got = b.tallies()
+        want = [np.concatenate([p.all_tallies()[k] for p in probs]) for k in range(4)]
+        for g, w in zip(got, want):
+            assert g.shape == w.shape and np.array_equal(g.view(np.uint64), w.view(np.uint64))
+        b.reset()
+        assert all(p.histories_run() == 0 for p in probs)
+        assert not np.any(b.tallies()[2]) and not np.any(b.tallies()[3])
+        b.upload()
+        b.run(seed=5)
+        again = b.tallies()
+        assert all(p.histories_run() == h for p, h in zip(probs, hist))
+        assert np.allclose(again[2], got[2], rtol=1e-12, atol=1e-300)   # same histories; atomics' order aside
+        b.close()
+        for p in probs:
+            p.close()
