@@ -314,9 +314,11 @@ mc_status mc_batch_run(mc_batch *b, uint64_t seed, const mc_tune *tune);
 /* Counters and device time of the last mc_batch_run (summed over problems). */
 mc_status mc_batch_counters(const mc_batch *b, mc_counters *out);
 /* Times each candidate launch shape on the batch with every problem's
- * histories scaled by sample_fraction (at least 64 each), then the
- * per-thread kernel's refill threshold among 2, 4, 8 and 16, and keeps the
- * fastest for runs with tune == NULL; the problems' tallies are untouched. */
+ * histories scaled by sample_fraction (at least 64 each) and keeps the
+ * fastest for runs with tune == NULL; the problems' tallies are untouched.
+ * The refill threshold keeps its default: the scaled sample holds a
+ * different mix of problem sizes, and a threshold it favours did not carry
+ * over to the whole batch. */
 mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double sample_fraction, mc_tune *out);
 /* Batch-wide forms of mc_problem_upload, mc_reset_tallies and mc_tally_read,
  * for callers that move every problem's tables and tallies at each run: the

@@ -203,21 +203,6 @@ mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double frac, mc_tune *ou
             const float ms = (float)batch_counters(trial).transport_ms;
             if (ms < best_ms) { best_ms = ms; best = t; }
         }
-        // the per-thread kernel's refill threshold, as for a single problem:
-        // another value replaces the default only when 2 % faster
-        if (st == MC_OK && best.kernel == 2) {
-            const mc_tune shape = best;
-            const float shape_ms = best_ms;
-            for (uint32_t r : {2u, 4u, 8u, 16u}) {
-                mc_tune t = shape;
-                t.refill = r;
-                std::string e2;
-                const mc_status s2 = batch_run(trial, b->sms, seed, &t, none, e2);
-                if (s2 != MC_OK) { st = s2; b->err = e2; break; }
-                const float ms = (float)batch_counters(trial).transport_ms;
-                if (ms < best_ms && ms < 0.98f * shape_ms) { best_ms = ms; best = t; }
-            }
-        }
     }
     batch_state_free(trial);
     cudaFree(pool);

@@ -109,7 +109,7 @@ def test_autotune_single_and_batch(mc):
         b = mc.Batch(probs, hist)
         t = b.autotune(fraction=0.05)
         assert t["kernel"] in (1, 2)
-        assert t["kernel"] == 1 or t["refill"] in (0, 2, 4, 8, 16)
+        assert t["refill"] == 0
         assert all(p.histories_run() == 0 for p in probs)
         b.run(seed=3)
         assert all(p.histories_run() == h for p, h in zip(probs, hist))
