@@ -52,7 +52,9 @@ roofline_l2  the same algorithmic bytes against an L2 read bandwidth measured
 roofline_issue  the kernel against its issue bound: warp instructions per
            history from the committed ncu capture of the same workload and
            launch shape x histories/s, over 4 schedulers per SM x the sampled
-           SM clock (the bound these latency-bound kernels actually have).
+           SM clock (the bound these latency-bound kernels actually have),
+           with the capture's warp execution efficiency (active threads per
+           warp instruction / 32).
 cpu_baseline  the CPU oracle (a C restatement of the reference's history
            loop) on one host core, on a bounded sample (~10 s) of the same
            workload.
@@ -295,8 +297,10 @@ def _issue_roofline(prof, leg, tuned, hist_per_s, clocks, sms):
         return None
     peak = sms * 4 * mhz * 1e6
     achieved = ipt * hist_per_s
+    thr = prof.get(leg["prof"] + "threads:k_track:%d" % tuned["blocks_per_sm"])
     return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
             "frac": achieved / peak, "warp_instructions_per_history": ipt,
+            "warp_execution_efficiency": thr / 32.0 if thr else None,
             "peak_source": f"{sms} SMs x 4 schedulers x {mhz:.0f} MHz (sampled)"}
 
 
