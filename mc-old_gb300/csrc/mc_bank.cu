@@ -322,6 +322,7 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_collide(const EvTables V, c
             const float4 x = B.fx[s];
             const int2 l = B.fl[s];
             R.init(A.seed, B.hidx[p.hslot], p.id, p.ev, 1u);
+            R.prime();   // the event's first block, inline (the collision draws from it)
             Flight f;
             f.sig = x.x;
             f.ss = x.y;
