@@ -365,14 +365,82 @@ def cpu_oracle_sample(d: str, seconds: float, first: int):
         n = int(n * min(20.0, max(2.0, seconds / max(dt, 1e-3))))
 
 
+def cpu_batch_sample(specs, seconds: float, procs: int = 1, start: int = 0, cap: int = 20_000):
+    """The CPU oracle on problems of a batch taken in a seeded random order
+    from position `start` (each run for min(histories, cap) histories), with
+    `procs` processes, until about `seconds` of CPU time per process.  The
+    batch's histories per problem are drawn independently of its geometry,
+    so the batch's CPU time on one core is estimated as its total histories
+    times the sampled problems' mean CPU time per history, and the problems,
+    being independent, spread over `procs` cores.  Returns (histories/s of
+    the whole batch on `procs` cores, problems sampled, histories run)."""
+    import numpy as np
+    from oracle import problem as OP
+    OP.build()
+    order = np.random.default_rng(SEED).permutation(len(specs))
+    order = np.concatenate([order[start % len(order):], order[:start % len(order)]])
+    per_hist, busy, ran, k = [], 0.0, 0, 0
+    pool = mp.get_context("spawn").Pool(procs) if procs > 1 else None
+    try:
+        while busy < seconds * procs and k < len(order):
+            chunk = order[k:k + 2 * procs]
+            k += len(chunk)
+            jobs = [(specs[i][0], 0, int(min(specs[i][1], cap)), SEED) for i in chunk]
+            res = pool.map(_oracle_worker, jobs, chunksize=1) if pool else [_oracle_worker(j) for j in jobs]
+            for j, (dt, _) in zip(jobs, res):
+                per_hist.append(dt / j[2])
+                busy += dt
+                ran += j[2]
+    finally:
+        if pool:
+            pool.close()
+            pool.join()
+    total = sum(h for _, h in specs)
+    t_one_core = total * statistics.mean(per_hist)
+    return total / (t_one_core / procs), len(per_hist), ran
+
+
+def reference_batch_arm(a):
+    """The batch on the host cores: the reference runs one Simulator per
+    problem, so the problems spread over one oracle process per core; each
+    step samples about ref-seconds of CPU time per process (cpu_batch_sample)."""
+    from mcgpu import workloads as W
+    procs = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as tmp:
+        specs = W.batch_shields(tmp, n_problems=a.batch_problems)
+        if a.warmup:
+            cpu_batch_sample(specs, 0.2, procs, start=len(specs) // 2)
+        rates, sampled, ran = [], 0, 0
+        for k in range(a.steps):
+            r, s_k, n_k = cpu_batch_sample(specs, a.ref_seconds, procs, start=k * 977)
+            rates.append(r)
+            sampled += s_k
+            ran += n_k
+    total = sum(h for _, h in specs)
+    v = statistics.mean(rates)
+    sample = (f"{sampled} problems of the batch in a seeded random order over {a.steps} steps, each run for "
+              f"min(its histories, 20000) histories ({ran} in all) through the C oracle (restated reference "
+              f"history loop, FP64), one process per core; the batch's CPU time is its {total} histories times "
+              "the sampled mean CPU time per history, divided over the cores")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "histories/s",
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * total / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"batch_shields: {len(specs)} MG slab/sphere shields, {total} histories, "
+                                   "one problem at a time per host core",
+                       "l2": "tables are L2-resident by design"},
+            "cpu_baseline": {"value": v, "unit": "histories/s", "cores": procs, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
 def reference_arm(a):
     rank, world, _ = _env_rank()
     if rank != 0:
         return 0
     if a.workload == "batch":
-        print(json.dumps({"impl": "reference", "unavailable": "the batch workload has no CPU reference arm "
-                          "(the reference runs one Simulator at a time); the single-problem legs have one"}))
-        return 0
+        return reference_batch_arm(a)
     leg = LEGS[a.workload]
     procs = os.cpu_count() or 1
     with tempfile.TemporaryDirectory() as tmp:
@@ -672,6 +740,14 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
         b.close()
         for p in probs:
             p.close()
+        cpu = None
+        if a.cpu_baseline:
+            r1, s1, n1 = cpu_batch_sample(specs, a.cpu_seconds, 1)
+            cpu = {"value": r1, "unit": "histories/s", "cores": 1, "kind": "port",
+                   "sample": f"{s1} problems of the batch in a seeded random order, each run for min(its "
+                             f"histories, 20000) histories ({n1} in all) through the C oracle (restated "
+                             "reference history loop, FP64), one core; the batch's CPU time is its histories "
+                             "times the sampled mean CPU time per history"}
     total = sum(hist)
     peaks, peak_kind = _measured_peaks()
     peak = float(peaks.get("hbm_gbs", 6800.0))
@@ -695,10 +771,15 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
                          "frac": achieved / peak if peak else None, "traffic": None,
                          "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs",
                          "algorithmic_bytes_per_step": alg_bytes},
+            "roofline_issue": _issue_roofline(_ncu_traffic(), {"prof": "batch/" if len(hist) == 4096 else "batch%d/" % len(hist)},
+                                              tuned, total / T, clocks,
+                                              torch.cuda.get_device_properties(0).multi_processor_count),
             "counters_per_step": {k: v / a.steps for k, v in cnt_sum.items()},
             "e2e": {"value": total * a.e2e_steps / e2e_t if a.e2e_steps else None, "unit": "histories/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clocks, "gpu_launches": launches}
+    if cpu:
+        line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line))
     return 0

@@ -265,9 +265,18 @@ __device__ __forceinline__ void store_p(const Tile &T, int s, const PState &p)
 // Per-thread event counters live in shared memory, one column per thread
 // (conflict-free), which keeps nine registers free for the transport itself.
 constexpr int kCntStride = 256;   // at least the threads per CTA of either kernel
+struct CounterRef {
+    uint32_t *p;
+    // an increment is one shared-memory atomic whose result nobody waits for,
+    // instead of a load, an add and a store
+    __device__ __forceinline__ void operator++(int) const { atomicAdd(p, 1u); }
+    __device__ __forceinline__ void operator+=(uint32_t v) const { atomicAdd(p, v); }
+    __device__ __forceinline__ void operator=(uint32_t v) const { *p = v; }
+    __device__ __forceinline__ operator uint32_t() const { return *p; }
+};
 struct Counters {
     uint32_t *base;               // this thread's column
-    __device__ __forceinline__ uint32_t &operator[](int k) const { return base[k * kCntStride]; }
+    __device__ __forceinline__ CounterRef operator[](int k) const { return CounterRef{base + k * kCntStride}; }
 };
 
 struct Ctx {

@@ -61,3 +61,32 @@ def test_reference_arm_runs_every_single_problem_workload():
         assert r.returncode == 0, r.stdout + r.stderr
         line = json.loads([l for l in r.stdout.splitlines() if l.strip().startswith("{")][0])
         assert line["impl"] == "reference" and line["value"] > 0 and w in line["config"]["workload"]
+
+
+def test_reference_arm_runs_the_batch():
+    """The batch on the host cores: one oracle process per core over a
+    seeded random sample of its problems."""
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0", "--ref-seconds", "0.2", "--workload", "batch", "--batch-problems", "16"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stdout + r.stderr
+    line = json.loads([l for l in r.stdout.splitlines() if l.strip().startswith("{")][0])
+    assert line["impl"] == "reference" and line["value"] > 0 and "batch_shields: 16" in line["config"]["workload"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"]["value"] == line["value"]
+
+
+def test_batch_cpu_estimate_arithmetic(monkeypatch):
+    """The batch's CPU time = its histories x the sampled problems' mean CPU
+    time per history, spread over the cores: with every sampled problem at
+    a known time per history the rate is cores / mean."""
+    sys.path.insert(0, ROOT)
+    import bench
+    per = {"a": 1e-6, "b": 3e-6, "c": 2e-6, "d": 2e-6}
+    monkeypatch.setattr(bench, "_oracle_worker", lambda job: (per[job[0]] * job[2], 0))
+    import oracle.problem as OP
+    monkeypatch.setattr(OP, "build", lambda: None)
+    specs = [("a", 100), ("b", 10_000_000), ("c", 5000), ("d", 70)]
+    rate, sampled, ran = bench.cpu_batch_sample(specs, 1e9, procs=1, cap=1000)
+    assert sampled == 4 and ran == 100 + 1000 + 1000 + 70
+    assert abs(rate - 1.0 / 2e-6) < 1e-6 * rate
