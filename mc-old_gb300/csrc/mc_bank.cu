@@ -112,7 +112,7 @@ __device__ __forceinline__ void bank_ctx(Ctx &C, const EvTables &V, const EvArgs
     C.tmask1 = 0ull;
     C.cbin = -1;
     C.cval = 0.0;
-    C.cnt.base = s_cnt + threadIdx.x;
+    C.cnt.base = cnt_column(s_cnt, threadIdx.x);
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
 }
 
@@ -132,7 +132,7 @@ __device__ __forceinline__ void bank_flush(const BankArgs &B, uint32_t *s_cnt, i
     __shared__ unsigned long long s_red[kBankBlock / 32][kNumCounters];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = 0; i < kNumCounters; ++i) {
-        unsigned long long v = s_cnt[i * kCntStride + threadIdx.x];
+        unsigned long long v = cnt_column(s_cnt, threadIdx.x)[i * kCntStride];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) s_red[warp][i] = v;
     }
@@ -192,7 +192,7 @@ __device__ __forceinline__ void bank_retire(Ctx &C, const BankArgs &B, bool dies
 template <int kFl>
 __global__ void __launch_bounds__(kBankBlock) k_bank_advance(const EvTables V, const EvArgs A, const BankArgs B)
 {
-    __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
+    __shared__ uint32_t s_cnt[cnt_words(kBankBlock)];
     __shared__ int s_status, s_go, s_more;
     const volatile BankCtl *vc = B.ctl;
     if (threadIdx.x == 0) {
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_advance(const EvTables V, c
 template <int kFl>
 __global__ void __launch_bounds__(kBankBlock) k_bank_collide(const EvTables V, const EvArgs A, const BankArgs B)
 {
-    __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
+    __shared__ uint32_t s_cnt[cnt_words(kBankBlock)];
     __shared__ int s_status, s_go;
     const volatile BankCtl *vc = B.ctl;
     if (threadIdx.x == 0) {
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(kBankBlock) k_bank_collide(const EvTables V, c
 template <int kFl>
 __global__ void __launch_bounds__(kBankBlock) k_bank_cross(const EvTables V, const EvArgs A, const BankArgs B)
 {
-    __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
+    __shared__ uint32_t s_cnt[cnt_words(kBankBlock)];
     __shared__ int s_status, s_go;
     const volatile BankCtl *vc = B.ctl;
     if (threadIdx.x == 0) {

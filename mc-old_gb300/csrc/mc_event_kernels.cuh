@@ -264,7 +264,16 @@ __device__ __forceinline__ void store_p(const Tile &T, int s, const PState &p)
 
 // Per-thread event counters live in shared memory, one column per thread
 // (conflict-free), which keeps nine registers free for the transport itself.
-constexpr int kCntStride = 256;   // at least the threads per CTA of either kernel
+// Threads come in banks of 128: counter k of thread t is word
+// [t / 128][k][t % 128], so a 128-thread block keeps 128 columns, not the
+// 256 a wider block needs.
+constexpr int kCntStride = 128;
+__device__ __forceinline__ uint32_t *cnt_column(uint32_t *s_cnt, int t)
+{
+    return s_cnt + (t / kCntStride) * (kNumCounters * kCntStride) + (t % kCntStride);
+}
+// words of the counter array of a block of `threads` threads
+__host__ __device__ constexpr int cnt_words(int threads) { return (threads + kCntStride - 1) / kCntStride * kNumCounters * kCntStride; }
 struct CounterRef {
     uint32_t *p;
     // an increment is one shared-memory atomic whose result nobody waits for,
@@ -1318,8 +1327,8 @@ __global__ void __launch_bounds__(256, MinB) k_event(const EvTables V0, const Ev
     C.tmask1 = 0ull;
     C.cbin = -1;
     C.cval = 0.0;
-    __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
-    C.cnt.base = s_cnt + threadIdx.x;
+    __shared__ uint32_t s_cnt[cnt_words(256)];
+    C.cnt.base = cnt_column(s_cnt, threadIdx.x);
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
     auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
     auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
@@ -1610,8 +1619,8 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
     C.tmask1 = 0ull;
     C.cbin = -1;
     C.cval = 0.0;
-    __shared__ uint32_t s_cnt[kNumCounters * kCntStride];
-    C.cnt.base = s_cnt + threadIdx.x;
+    __shared__ uint32_t s_cnt[cnt_words(kTrackBlock)];
+    C.cnt.base = cnt_column(s_cnt, threadIdx.x);
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
     auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
     auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
