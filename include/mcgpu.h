@@ -301,7 +301,10 @@ mc_status mc_backward_density(mc_problem *p, const double *params, uint64_t n_hi
  * runs every history of every problem in ONE launch of the event engine
  * (MC_MIXED_EVENT), replayed from a CUDA graph captured at the first run,
  * and folds each problem's results into that problem's tallies (read them
- * with mc_tally_read on the problem handles).  Problem i's histories use the
+ * with mc_tally_read on the problem handles).  Histories fold into up to 64
+ * copies of the batch's bins (one per group of CTAs, at most 256 MiB); a
+ * second kernel in the same graph adds the copies into the problems' sums
+ * and clears them, so the graph launches two kernels.  Problem i's histories use the
  * seed  seed + 0x9E3779B97F4A7C15 * (i + 1),  so they are the histories an
  * mc_run of that problem alone with that seed would follow.  The problems
  * must outlive the batch and must not be run on their own while a batch run

@@ -82,6 +82,30 @@ size_t tile_smem_bytes(int P, long long nb_smem)
     return (size_t)P * (8 + 4 * TA_COUNT + 2 * sizeof(unsigned short)) + sizeof(double) * 2 * (size_t)nb_smem + 64;
 }
 
+// The replicas of a batch's sums into each problem's sums (fixed order over
+// the replicas), and the replicas back to zero for the next run.
+__global__ void k_batch_reduce(const EvArgs A, const int *rep_prob)
+{
+    const long long stride = A.rep_stride;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < stride;
+         j += (long long)gridDim.x * blockDim.x) {
+        double s = 0.0, q = 0.0;
+        for (int k = 0; k < A.n_rep; ++k) {
+            const size_t at = (size_t)k * (size_t)stride + (size_t)j;
+            s += A.rsum[at];
+            q += A.rsq[at];
+            A.rsum[at] = 0.0;
+            A.rsq[at] = 0.0;
+        }
+        if (s != 0.0 || q != 0.0) {
+            const int p = rep_prob[j];
+            const long long bin = j - A.rep_off[p];
+            A.psum[p][bin] += s;
+            A.psq[p][bin] += q;
+        }
+    }
+}
+
 EvKernel pick_kernel(int minb, bool batch, int kernel, int flavor)
 {
     if (kernel == 2) {
@@ -155,6 +179,12 @@ cudaError_t event_tables_upload_async(DeviceProblem &d, cudaStream_t st)
 size_t event_table_bytes(const DeviceProblem &d) { return d.ev_state ? d.ev_state->blob_bytes : 0; }
 
 const EvTables &event_tables_view(const DeviceProblem &d) { return d.ev_state->dv; }
+
+// A batch folds its histories into kBatchReplicas copies of its sums (fewer
+// where the copies would take more than kBatchReplicaBytes): one copy per
+// group of CTAs, added into the problems' sums after the launch.
+constexpr long long kBatchReplicas = 64;
+constexpr size_t kBatchReplicaBytes = (size_t)256 << 20;
 
 // Launch geometry of the event kernel for a tune (0 fields = tuned / defaults).
 struct EvLaunch {
@@ -394,7 +424,11 @@ struct BatchState {
     std::vector<uint64_t> hist;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
-    DevBuf meta;                      // tabs, prefix, seeds, psum, psq
+    DevBuf meta;                      // tabs, prefix, seeds, psum, psq, rep_off, rep_prob
+    DevBuf rep;                       // the replicas of the batch's sums: [2][n_rep][rep_stride]
+    int n_rep = 1;
+    long long rep_stride = 1;         // bins of all problems
+    bool rep_dirty = false;           // a run stopped before k_batch_reduce cleared the replicas
     EventState scratch;               // rows / mask / overflow / control
     long long row_nb = 1;
     uint64_t total = 0;
@@ -414,6 +448,7 @@ void batch_state_free(BatchState *b)
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     devbuf_free(b->meta);
+    devbuf_free(b->rep);
     devbuf_free(b->scratch.acc);
     devbuf_free(b->scratch.mask);
     devbuf_free(b->scratch.ovf);
@@ -457,6 +492,16 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
     }
     b->flavor = any_time ? FL_ALL : (all_mg ? FL_MG : (all_ce ? FL_CE : FL_ALL));
     b->total = prefix[n];
+    // replicas of every problem's bins: kBatchReplicas copies, fewer where
+    // they would pass kBatchReplicaBytes
+    std::vector<long long> rep_off(n + 1, 0);
+    for (uint32_t i = 0; i < n; ++i) rep_off[i + 1] = rep_off[i] + std::max<long long>(views[i].n_bins, 0);
+    b->rep_stride = std::max<long long>(rep_off[n], 1);
+    std::vector<int> rep_prob((size_t)b->rep_stride, 0);
+    for (uint32_t i = 0; i < n; ++i)
+        for (long long j = rep_off[i]; j < rep_off[i + 1]; ++j) rep_prob[(size_t)j] = (int)i;
+    b->n_rep = (int)std::max<long long>(
+        1, std::min<long long>(kBatchReplicas, (long long)(kBatchReplicaBytes / (2 * sizeof(double) * (size_t)b->rep_stride))));
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         batch_state_free(b);
@@ -464,8 +509,11 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
         return MC_ERR_CUDA;
     }
     for (auto &ev : b->ev) cudaEventCreate(&ev);
-    const size_t sz = n * sizeof(EvTables) + (n + 1) * 8 + n * 8 + 2 * n * sizeof(double *) + 6 * 256;
-    if (!devbuf_reserve(b->meta, sz) || cudaHostAlloc(&b->h_seeds, n * 8, cudaHostAllocDefault) != cudaSuccess) {
+    const size_t sz = n * sizeof(EvTables) + (n + 1) * 8 + n * 8 + 2 * n * sizeof(double *) + (n + 1) * 8 +
+                      (size_t)b->rep_stride * sizeof(int) + 8 * 256;
+    const size_t rep_bytes = 2 * sizeof(double) * (size_t)b->n_rep * (size_t)b->rep_stride;
+    if (!devbuf_reserve(b->meta, sz) || !devbuf_reserve(b->rep, rep_bytes) ||
+        cudaHostAlloc(&b->h_seeds, n * 8, cudaHostAllocDefault) != cudaSuccess) {
         batch_state_free(b);
         err = "cannot allocate batch descriptors";
         return MC_ERR_NOMEM;
@@ -485,6 +533,11 @@ mc_status batch_create(const std::vector<const Tables *> &tabs, const std::vecto
     put(prefix.data(), (n + 1) * 8);
     put(psum.data(), n * sizeof(double *));
     put(psq.data(), n * sizeof(double *));
+    off = (off + 255) & ~(size_t)255;
+    off += n * 8;   // the seeds (written by each run)
+    put(rep_off.data(), (n + 1) * sizeof(long long));
+    put(rep_prob.data(), (size_t)b->rep_stride * sizeof(int));
+    if (put_err == cudaSuccess) put_err = cudaMemset(b->rep.ptr, 0, rep_bytes);
     if (put_err != cudaSuccess) {
         batch_state_free(b);
         err = cuda_msg(put_err, "batch descriptors");
@@ -518,7 +571,15 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     double *const *d_psum = reinterpret_cast<double *const *>(at(n * sizeof(double *)));
     double *const *d_psq = reinterpret_cast<double *const *>(at(n * sizeof(double *)));
     unsigned long long *d_seeds = reinterpret_cast<unsigned long long *>(at(n * 8));
+    const long long *d_rep_off = reinterpret_cast<const long long *>(at((n + 1) * sizeof(long long)));
+    const int *d_rep_prob = reinterpret_cast<const int *>(at((size_t)b->rep_stride * sizeof(int)));
+    double *d_rsum = static_cast<double *>(b->rep.ptr);
+    double *d_rsq = d_rsum + (size_t)b->n_rep * (size_t)b->rep_stride;
     cudaError_t e;
+    if (b->rep_dirty) {
+        cudaMemsetAsync(b->rep.ptr, 0, 2 * sizeof(double) * (size_t)b->n_rep * (size_t)b->rep_stride, b->stream);
+        b->rep_dirty = false;
+    }
     if (!same_shape) {
         if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
         char *misc = static_cast<char *>(b->scratch.misc.ptr);
@@ -545,6 +606,11 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         A.psum = d_psum;
         A.psq = d_psq;
         A.n_prob = (int)n;
+        A.rsum = d_rsum;
+        A.rsq = d_rsq;
+        A.rep_off = d_rep_off;
+        A.rep_stride = b->rep_stride;
+        A.n_rep = b->n_rep;
         EvTables V0{};
         V0.n_bins = 0;
         // capture: seeds (pinned host -> device), control reset, the launch
@@ -556,6 +622,8 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         cudaMemcpyAsync(d_seeds, b->h_seeds, n * 8, cudaMemcpyHostToDevice, b->stream);
         cudaMemsetAsync(misc, 0, 256 + kNumCounters * sizeof(unsigned long long), b->stream);
         pick_kernel(L.minb, true, L.kernel, L.flavor)<<<L.grid, L.block, L.smem, b->stream>>>(V0, A);
+        const int rgrid = (int)std::min<long long>((b->rep_stride + 255) / 256, 4LL * device_sms);
+        k_batch_reduce<<<rgrid, 256, 0, b->stream>>>(A, d_rep_prob);
         if ((e = cudaStreamEndCapture(b->stream, &g)) != cudaSuccess) {
             err = cuda_msg(e, "graph capture end");
             return MC_ERR_CUDA;
@@ -567,7 +635,11 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         b->have_shape = true;
     }
     cudaEventRecord(b->ev[0], b->stream);
-    if ((e = cudaGraphLaunch(b->exec, b->stream)) != cudaSuccess) { err = cuda_msg(e, "graph launch"); return MC_ERR_CUDA; }
+    if ((e = cudaGraphLaunch(b->exec, b->stream)) != cudaSuccess) {
+        b->rep_dirty = true;
+        err = cuda_msg(e, "graph launch");
+        return MC_ERR_CUDA;
+    }
     cudaEventRecord(b->ev[1], b->stream);
     char *misc = static_cast<char *>(b->scratch.misc.ptr);
     int hs = 0;
@@ -577,6 +649,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
         (e = cudaStreamSynchronize(b->stream)) != cudaSuccess) {
         err = cuda_msg(e, "batch kernel");
         b->scratch.rows_dirty = true;
+        b->rep_dirty = true;
         return MC_ERR_CUDA;
     }
     float ms = 0.f;
@@ -592,7 +665,7 @@ mc_status batch_run(BatchState *b, int device_sms, uint64_t seed, const mc_tune 
     b->last.histories = b->total;
     b->last.transport_ms = ms;
     b->last.total_ms = ms;
-    b->last.launches = 1;
+    b->last.launches = 2;   // the transport kernel and k_batch_reduce
     if (b->count_histories)
         for (uint32_t i = 0; i < n; ++i) {
             b->probs[i]->histories += b->hist[i];

@@ -35,7 +35,7 @@ def test_batch_equals_problems_run_alone(mc, kernel):
         b = mc.Batch(probs, hist)
         c = b.run(seed=seed, kernel=kernel)
         assert c["histories"] == sum(hist)
-        assert c["launches"] == 1
+        assert c["launches"] == 2   # the transport kernel and the fold of the replicated sums
         batch_res = [p.all_tallies() for p in probs]
         for i, p in enumerate(probs):
             assert p.histories_run() == hist[i]
@@ -141,5 +141,35 @@ def test_batch_wide_upload_reset_and_read(mc):
         assert all(p.histories_run() == h for p, h in zip(probs, hist))
         assert np.allclose(again[2], got[2], rtol=1e-12, atol=1e-300)   # same histories; atomics' order aside
         b.close()
+        for p in probs:
+            p.close()
+
+
+def test_batch_replicated_sums_equal_lone_runs(mc):
+    """A batch folds histories into replicas of its sums (a copy per group
+    of CTAs) and adds them into each problem's sums after the launch: a
+    batch of a few problems of 2*10^5 histories each gives what lone runs
+    give, and a second run adds to the first (the replicas were cleared)."""
+    import mcgpu.workloads as W
+    seed = 4242
+    with tempfile.TemporaryDirectory() as root:
+        specs = W.batch_shields(root, n_problems=3, min_hist=200000, max_hist=200001)
+        probs = [mc.Problem(d) for d, _ in specs]
+        hist = [h for _, h in specs]
+        b = mc.Batch(probs, hist)
+        b.run(seed=seed)
+        first = [p.all_tallies() for p in probs]
+        b.run(seed=seed + 1)
+        second = [p.all_tallies() for p in probs]
+        b.close()
+        for i, p in enumerate(probs):
+            assert p.histories_run() == 2 * hist[i]
+            # the sums of the second run add to the first's
+            assert np.all(second[i][2] >= first[i][2] - 1e-12)
+            p.reset()
+            p.run(n=hist[i], seed=mc.batch_problem_seed(seed, i), mode="event")
+            m2, s2, su2, _ = p.all_tallies()
+            assert np.allclose(first[i][2], su2, rtol=1e-6, atol=1e-12), f"problem {i}"
+            assert_agree(first[i][0], first[i][1], m2, s2, f"problem {i}")
         for p in probs:
             p.close()
