@@ -81,7 +81,6 @@ enum Flavor { FL_ALL = 0, FL_CE = 1, FL_MG = 2, FL_MGB = 3 };
 // 128 threads per CTA lets the register budget step through 128 / 80 / 72 /
 // 64 registers (4 / 6 / 7 / 8 CTAs per SM)
 constexpr int kTrackBlock = 128;
-constexpr uint32_t kBatchChunk = 8;   // histories a lane takes at once in a batch
 constexpr int kTrackDepth = 32;   // default split copies a thread keeps pending
 
 typedef void (*EvKernel)(const EvTables, const EvArgs);
@@ -1651,10 +1650,8 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
     uint64_t hist = 0;
     int prob = 0;
     uint32_t walks = 0;   // particles of the current history (bounded)
-    // batches: the lane's chunk of consecutive histories and the bounds of
-    // the problem of the last one
-    unsigned long long chunk_next = 0, prob_lo = 1, prob_hi = 0;
-    uint32_t chunk_left = 0;
+    // batches: the bounds of the problem of the lane's last history
+    unsigned long long prob_lo = 1, prob_hi = 0;
     // split copies wait on the thread's own stack
     auto push = [&](const PState &q, uint32_t cid) -> bool {
         if (sp >= depth) return false;
@@ -1698,59 +1695,35 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
             open = false;
         }
         const bool need = refill && idle;
-        if constexpr (!kBatch) {
-            const unsigned m = __ballot_sync(0xffffffffu, need);
-            if (m) {
-                const int leader = __ffs(m) - 1;
-                unsigned long long base = 0;
-                if (lane == leader) base = atomicAdd(A.next, (unsigned long long)__popc(m));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (need) {
-                    const unsigned long long gi = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
-                    if (gi >= A.n) {
-                        exhausted = true;
-                    } else {
-                        prob = 0;
-                        hist = A.first + gi;
-                        sample_source(V0, A.seed, hist, p);
-                        p.hslot = hslot;
-                        p.prob = 0;
-                        have = true;
-                        open = true;
-                        walks = 1;
-                        C.cnt[C_PART]++;
-                    }
-                }
-            }
-        } else {
-            // a lane takes kBatchChunk consecutive histories of the batch at a
-            // time, so the next history's problem is usually the one whose
-            // bounds it holds, and the bisection over the problems runs
-            // about once per chunk
-            const bool grab = need && chunk_left == 0;
-            const unsigned m = __ballot_sync(0xffffffffu, grab);
-            if (m) {
-                const int leader = __ffs(m) - 1;
-                unsigned long long base = 0;
-                if (lane == leader) base = atomicAdd(A.next, (unsigned long long)__popc(m) * kBatchChunk);
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (grab) {
-                    chunk_next = base + (unsigned long long)__popc(m & ((1u << lane) - 1u)) * kBatchChunk;
-                    chunk_left = kBatchChunk;
-                }
-            }
+        // the warp's lanes that need a history take consecutive ones, one
+        // each, with one atomic.  In a batch the history index runs over the
+        // concatenated problems: a lane looks its problem up when the index
+        // leaves the bounds of the last one.  (Taking several consecutive
+        // histories per lane, to look problems up less often, lengthens the
+        // end of the launch: the last problems' histories then run several
+        // to a lane, one after another.)
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(A.next, (unsigned long long)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
             if (need) {
-                const unsigned long long gi = chunk_next++;
-                --chunk_left;
+                const unsigned long long gi = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
                 if (gi >= A.n) {
                     exhausted = true;
                 } else {
-                    if (!(gi >= prob_lo && gi < prob_hi)) {
-                        prob = problem_of(A, gi);
-                        prob_lo = A.prefix[prob];
-                        prob_hi = A.prefix[prob + 1];
+                    if constexpr (kBatch) {
+                        if (!(gi >= prob_lo && gi < prob_hi)) {
+                            prob = problem_of(A, gi);
+                            prob_lo = A.prefix[prob];
+                            prob_hi = A.prefix[prob + 1];
+                        }
+                        hist = gi - prob_lo;
+                    } else {
+                        prob = 0;
+                        hist = A.first + gi;
                     }
-                    hist = gi - prob_lo;
                     sample_source(tab(prob), seed_of(prob), hist, p);
                     p.hslot = hslot;
                     p.prob = prob;
