@@ -264,7 +264,10 @@ static mc_status event_launch_shape(const DeviceProblem &d, const mc_tune *tune,
             return MC_ERR_ARG;
         }
         L.ovf_cap = kTrackBlock * depth;
+        // the per-CTA sums, then (multigroup, with them) every thread's
+        // running sums of its register bin and that bin
         L.smem = sizeof(double) * 2 * (size_t)nb_smem + 64;
+        if (nb_smem > 0 && flavor == FL_MG) L.smem += kTrackBlock * (2 * sizeof(double) + sizeof(int));
     } else {
         L.tile = (tune && tune->bank_capacity) ? (int)tune->bank_capacity
                : (tuned.bank_capacity ? (int)tuned.bank_capacity : 512);

@@ -244,6 +244,10 @@ struct Tile {
         return reinterpret_cast<double *>(base + 8 * P + 4 * P * TA_COUNT + 4 * P);
     }
     __device__ __forceinline__ double *ssq() const { return ssum() + nsum; }
+    // multigroup k_track with per-CTA sums: each thread's running sum and
+    // sum of squares of its register bin ([kTrackBlock][2]), then that bin
+    __device__ __forceinline__ double *lane_acc() const { return ssq() + nsum; }
+    __device__ __forceinline__ int *lane_bin() const { return reinterpret_cast<int *>(lane_acc() + 2 * kTrackBlock); }
 };
 
 struct PState {
@@ -768,8 +772,24 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
         if (C.cbin >= 0) {
             const double v = C.cval;
             if (C.A->smem_sums) {
-                atomicAdd(C.T.ssum() + C.cbin, v);
-                atomicAdd(C.T.ssq() + C.cbin, v * v);
+                // the thread's own running sums of the bin (no other thread
+                // touches them; most of a thread's histories score the same
+                // bin): the CTA's sums take a pair of shared-memory atomics
+                // when the bin changes, not one per history
+                double *la = C.T.lane_acc() + 2 * threadIdx.x;
+                int *lb = C.T.lane_bin() + threadIdx.x;
+                if (*lb == C.cbin) {
+                    la[0] += v;
+                    la[1] += v * v;
+                } else {
+                    if (*lb >= 0) {
+                        atomicAdd(C.T.ssum() + *lb, la[0]);
+                        atomicAdd(C.T.ssq() + *lb, la[1]);
+                    }
+                    *lb = C.cbin;
+                    la[0] = v;
+                    la[1] = v * v;
+                }
             } else {
                 atomicAdd(gs + C.cbin, v);
                 atomicAdd(gq + C.cbin, v * v);
@@ -1635,8 +1655,10 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
     for (int i = 0; i < kNumCounters; ++i) C.cnt[i] = 0;
     auto tab = [&](int prob) -> const EvTables & { return kBatch ? A.tabs[prob] : V0; };
     auto seed_of = [&](int prob) -> uint64_t { return kBatch ? A.seeds[prob] : A.seed; };
-    if (A.smem_sums)
+    if (A.smem_sums) {
         for (int b = threadIdx.x; b < 2 * V0.n_bins; b += blockDim.x) C.T.ssum()[b] = 0.0;
+        if constexpr (kFl == FL_MG) C.T.lane_bin()[threadIdx.x] = -1;
+    }
     if (threadIdx.x == 0) s_status = 0;
     __syncthreads();
 
@@ -1783,6 +1805,15 @@ __global__ void __launch_bounds__(kTrackBlock, MinB) k_track(const EvTables V0, 
         }
     }
 
+    if constexpr (kFl == FL_MG) {
+        if (A.smem_sums) {   // the thread's running sums into the CTA's
+            const int lb = C.T.lane_bin()[threadIdx.x];
+            if (lb >= 0) {
+                atomicAdd(C.T.ssum() + lb, C.T.lane_acc()[2 * threadIdx.x]);
+                atomicAdd(C.T.ssq() + lb, C.T.lane_acc()[2 * threadIdx.x + 1]);
+            }
+        }
+    }
     __syncthreads();
     if (A.smem_sums) {
         for (int b = threadIdx.x; b < V0.n_bins; b += blockDim.x) {
