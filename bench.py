@@ -686,7 +686,7 @@ def batch_arm(a, mcgpu, torch, flush, rank, world, dist):
         b = mcgpu.Batch(probs, hist)
         run_kw = {}
         if a.kernel == "auto":
-            tuned = b.autotune(seed=SEED + 17, fraction=0.01)
+            tuned = b.autotune(seed=SEED + 17, fraction=0.05)
         else:   # a fixed shape (profiling runs)
             mb = a.blocks_per_sm if a.blocks_per_sm is not None else (2 if a.kernel == "tile" else 8)
             tuned = {"kernel": 1 if a.kernel == "tile" else 2, "blocks_per_sm": mb,

@@ -317,8 +317,9 @@ mc_status mc_batch_run(mc_batch *b, uint64_t seed, const mc_tune *tune);
 /* Counters and device time of the last mc_batch_run (summed over problems). */
 mc_status mc_batch_counters(const mc_batch *b, mc_counters *out);
 /* Times each candidate launch shape on the batch with every problem's
- * histories scaled by sample_fraction (at least 64 each) and keeps the
- * fastest for runs with tune == NULL; the problems' tallies are untouched.
+ * histories scaled by sample_fraction (at least 64 each; 0 or out of
+ * (0, 1]: 0.05) and keeps the fastest for runs with tune == NULL; the
+ * problems' tallies are untouched.
  * The refill threshold keeps its default: the scaled sample holds a
  * different mix of problem sizes, and a threshold it favours did not carry
  * over to the whole batch. */

@@ -152,7 +152,9 @@ mc_status mc_batch_counters(const mc_batch *b, mc_counters *out)
 mc_status mc_batch_autotune(mc_batch *b, uint64_t seed, double frac, mc_tune *out)
 {
     if (!b || !b->state || !out) return MC_ERR_ARG;
-    if (!(frac > 0.0) || frac > 1.0) frac = 0.02;
+    // default 5 %: on a batch of 4096 uneven shields a 1 % sample picked 7
+    // CTAs per SM (391 ms for the batch), 3 % and more picked 8 (382 ms)
+    if (!(frac > 0.0) || frac > 1.0) frac = 0.05;
     const uint32_t n = (uint32_t)b->probs.size();
     std::vector<const Tables *> tabs;
     std::vector<DeviceProblem *> devs;

@@ -354,7 +354,7 @@ class Batch:
         self._check(lib().mc_batch_counters(self._h, ctypes.byref(c)))
         return c.as_dict()
 
-    def autotune(self, seed: int = DEFAULT_SEED, fraction: float = 0.02) -> dict:
+    def autotune(self, seed: int = DEFAULT_SEED, fraction: float = 0.05) -> dict:
         t = Tune()
         self._check(lib().mc_batch_autotune(self._h, seed, fraction, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
