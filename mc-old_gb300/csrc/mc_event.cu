@@ -60,6 +60,13 @@ struct EventState {
     int grid = 0, block = 0, tile = 0, ovf_cap = 0;
     size_t smem = 0;
     bool rows_dirty = true;
+    // a problem whose sums do not fit in shared memory: replicas of its
+    // sums ([2][n_rep][n_bins]) and what k_batch_reduce reads for one
+    // problem (the sums' pointers, rep_off = {0, n_bins}, rep_prob = 0)
+    DevBuf rep, rep_meta;
+    int n_rep = 0;
+    long long rep_stride = 0;
+    bool rep_dirty = false;
 };
 
 void event_state_free(EventState *s)
@@ -71,6 +78,8 @@ void event_state_free(EventState *s)
     devbuf_free(s->mask);
     devbuf_free(s->ovf);
     devbuf_free(s->misc);
+    devbuf_free(s->rep);
+    devbuf_free(s->rep_meta);
     delete s;
 }
 
@@ -336,6 +345,44 @@ static void fill_counters(mc_counters &L, const unsigned long long *cnt)
     L.nuc_lookups = cnt[8];
 }
 
+// Replicas of a single problem's sums when they do not fit in shared
+// memory (see EvArgs::n_rep); fills A's replica fields.
+static mc_status single_replicas(EventState &S, const DeviceProblem &d, long long nb, EvArgs &A,
+                                 const int *&rep_prob, std::string &err)
+{
+    const int n_rep = (int)std::max<long long>(
+        1, std::min<long long>(kBatchReplicas, (long long)(kBatchReplicaBytes / (2 * sizeof(double) * (size_t)nb))));
+    const size_t rep_bytes = 2 * sizeof(double) * (size_t)n_rep * (size_t)nb;
+    const size_t meta_bytes = 256 + (size_t)nb * sizeof(int);
+    if (!S.rep.ptr || S.n_rep != n_rep || S.rep_stride != nb) {
+        if (!devbuf_reserve(S.rep, rep_bytes) || !devbuf_reserve(S.rep_meta, meta_bytes)) {
+            err = "cannot allocate the replicated sums";
+            return MC_ERR_NOMEM;
+        }
+        S.n_rep = n_rep;
+        S.rep_stride = nb;
+        S.rep_dirty = true;
+    }
+    // the sums' pointers and rep_off = {0, nb} in the first 256 bytes, then rep_prob = 0
+    struct { double *ps, *pq; long long off[2]; } h{d.d_sum, d.d_sq, {0, nb}};
+    char *m = static_cast<char *>(S.rep_meta.ptr);
+    cudaMemcpyAsync(m, &h, sizeof(h), cudaMemcpyHostToDevice, d.stream);
+    if (S.rep_dirty) {
+        cudaMemsetAsync(m + 256, 0, (size_t)nb * sizeof(int), d.stream);
+        cudaMemsetAsync(S.rep.ptr, 0, rep_bytes, d.stream);
+        S.rep_dirty = false;
+    }
+    A.rsum = static_cast<double *>(S.rep.ptr);
+    A.rsq = A.rsum + (size_t)n_rep * (size_t)nb;
+    A.psum = reinterpret_cast<double *const *>(m);
+    A.psq = reinterpret_cast<double *const *>(m + sizeof(double *));
+    A.rep_off = reinterpret_cast<const long long *>(m + 2 * sizeof(double *));
+    A.rep_stride = nb;
+    A.n_rep = n_rep;
+    rep_prob = reinterpret_cast<const int *>(m + 256);
+    return MC_OK;
+}
+
 mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t n, uint64_t seed,
                     const mc_tune *tune, std::string &err)
 {
@@ -386,10 +433,18 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     A.smem_sums = smem_sums ? 1 : 0;
     A.refill_min = L.refill;
     A.n_prob = 0;
+    const int *d_rep_prob = nullptr;
+    if (!smem_sums && (st = single_replicas(S, d, nb, A, d_rep_prob, err)) != MC_OK) return st;
     cudaEventRecord(d.ev[0], d.stream);
     pick_kernel(L.minb, false, L.kernel, L.flavor)<<<L.grid, L.block, L.smem, d.stream>>>(V, A);
     cudaError_t e;
-    if ((e = cudaGetLastError()) != cudaSuccess) { err = cuda_msg(e, "event kernel launch"); return MC_ERR_CUDA; }
+    if ((e = cudaGetLastError()) != cudaSuccess) {
+        S.rep_dirty = A.n_rep > 0;
+        err = cuda_msg(e, "event kernel launch");
+        return MC_ERR_CUDA;
+    }
+    if (A.n_rep > 0)
+        k_batch_reduce<<<(int)std::min<long long>((nb + 255) / 256, 4LL * d.sms), 256, 0, d.stream>>>(A, d_rep_prob);
     cudaEventRecord(d.ev[1], d.stream);
     int hs = 0;
     unsigned long long cnt[kNumCounters];
@@ -398,6 +453,7 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
         (e = cudaStreamSynchronize(d.stream)) != cudaSuccess) {
         err = cuda_msg(e, "event kernel");
         S.rows_dirty = true;
+        S.rep_dirty = A.n_rep > 0;
         return MC_ERR_CUDA;
     }
     float ms = 0.f;
@@ -412,7 +468,7 @@ mc_status run_event(const Tables &t, DeviceProblem &d, uint64_t first, uint64_t 
     C.histories = n;
     C.transport_ms = ms;
     C.total_ms = ms;
-    C.launches = 1;
+    C.launches = A.n_rep > 0 ? 2 : 1;
     d.histories += n;
     d.ntrack += C.flights;
     d.exact_valid = false;   // the mixed mode keeps no per-history rows to sum exactly

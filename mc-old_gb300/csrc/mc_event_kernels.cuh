@@ -47,9 +47,10 @@ struct EvArgs {
     double *const *psum;          // [n_prob] per-problem tallies
     double *const *psq;
     int n_prob;
-    // batches fold histories into n_rep replicas of the batch's bins
-    // ([n_rep][rep_stride], problem p's bins from rep_off[p] on), each CTA
-    // into replica blockIdx % n_rep; k_batch_reduce adds them to psum / psq
+    // batches, and single problems whose sums do not fit in shared memory,
+    // fold histories into n_rep > 0 replicas of their bins ([n_rep]
+    // [rep_stride], problem p's bins from rep_off[p] on), each CTA into
+    // replica blockIdx % n_rep; k_batch_reduce adds them to psum / psq
     double *rsum, *rsq;
     const long long *rep_off;     // [n_prob + 1]
     long long rep_stride;
@@ -759,12 +760,13 @@ __device__ void history_fold(Ctx &C, int hslot, int prob)
     double *acc = C.A->acc + row * C.A->row_nb;
     unsigned long long *mask = C.A->mask + row * C.A->nw;
     double *gs = C.A->sum, *gq = C.A->sq;
-    if (C.A->n_prob > 0) {
-        // a batch: this CTA's replica of the problem's bins.  Histories of
-        // one problem fold at the same time all over the GPU; into one set
-        // of sums their FP64 additions to the same few addresses queue up
-        // at L2 (about 10^9 histories/s in all, whatever the problem).
-        const size_t at = (size_t)(blockIdx.x % C.A->n_rep) * (size_t)C.A->rep_stride + (size_t)C.A->rep_off[prob];
+    if (C.A->n_rep > 0) {
+        // this CTA's replica of the problem's bins.  Histories of one
+        // problem fold at the same time all over the GPU; into one set of
+        // sums their FP64 additions to the same few addresses queue up at
+        // L2 (a batch: about 10^9 histories/s in all, whatever the problem)
+        const size_t at = (size_t)(blockIdx.x % C.A->n_rep) * (size_t)C.A->rep_stride +
+                          (size_t)(C.A->n_prob > 0 ? C.A->rep_off[prob] : 0);
         gs = C.A->rsum + at;
         gq = C.A->rsq + at;
     }

@@ -251,3 +251,44 @@ def test_event_agrees_with_the_reference_run(mc, name):
         p.close()
     gm, gu = golden_arrays(g)
     assert_agree(m, s, gm, gu, f"{name}: mixed mode vs the reference")
+
+
+def test_many_bins_fold_through_replicated_sums(mc):
+    """Beyond 4096 bins a problem's sums do not fit in shared memory: its
+    histories fold into replicas of the sums, which a second kernel adds
+    into the problem's sums and clears.  On a 5002-bin slab the tile and
+    the per-thread kernels, which follow the same tracks, give the same
+    sums up to summation order, a second run adds to the first, and the
+    mixed mode agrees with FP64 replay: the reflected and transmitted
+    currents within combined 3 sigma, and the flux and absorption in 2500
+    cells of 0.008 mean free paths bin by bin (neighbouring bins are nearly
+    the same quantity, so a chi-square over them, which assumes independent
+    bins, does not apply; the fraction within 3 sigma does)."""
+    from stats import compare
+    import mcgpu.workloads as W
+    n = 100000
+    sums = {}
+    with tempfile.TemporaryDirectory() as d:
+        W.slab_1g(d, samples=10, n_flux_bins=2500)    # 2 x 2500 + 2 bins
+        p = mc.Problem(d, d + "/xs_library")
+        assert int(sum(p.sizes)) > 4096
+        for kernel in (1, 2):
+            p.reset()
+            c = p.run(n=n, mode="event", kernel=kernel)
+            assert c["launches"] == 2
+            half = p.all_tallies()[2].copy()
+            p.run(n=n, first=n, mode="event", kernel=kernel)
+            assert p.histories_run() == 2 * n
+            su1 = p.all_tallies()[2]
+            assert np.all(su1 >= half - 1e-12) and su1.sum() > half.sum()
+            sums[kernel] = su1
+        ev = {k: p.tally(p.names.index(k))[:2] for k in ("transmission", "reflection", "slab")}
+        p.reset()
+        p.run(n=2 * n, first=10 * n, mode="replay")
+        rp = {k: p.tally(p.names.index(k))[:2] for k in ("transmission", "reflection", "slab")}
+        p.close()
+    assert np.allclose(sums[1], sums[2], rtol=1e-9, atol=1e-300)
+    for k in ("transmission", "reflection"):
+        assert_agree(*ev[k], *rp[k], k)
+    frac, _, _, _ = compare(*ev["slab"], *rp["slab"])
+    assert frac >= 0.95, f"slab flux / absorption: {frac:.3f} of bins within 3 sigma"
