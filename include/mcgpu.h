@@ -119,7 +119,10 @@ typedef struct {
     double   transport_ms;    /* device time of the transport kernels */
     double   fold_ms;         /* device time of the history fold */
     double   total_ms;        /* device time of the whole mc_run */
-    uint32_t launches;        /* kernels launched by the last mc_run */
+    uint32_t launches;        /* kernels launched by the last mc_run (mixed
+                                 mode: 2 where a second kernel adds the
+                                 replicated sums of a problem of more than
+                                 4096 bins, or of a batch) */
     uint32_t reserved;        /* 0 (pads the struct to 8 bytes) */
 } mc_counters;
 
@@ -304,8 +307,9 @@ mc_status mc_backward_density(mc_problem *p, const double *params, uint64_t n_hi
  * with mc_tally_read on the problem handles).  Histories fold into up to 64
  * copies of the batch's bins (one per group of CTAs, at most 256 MiB); a
  * second kernel in the same graph adds the copies into the problems' sums
- * and clears them, so the graph launches two kernels.  Problem i's histories use the
- * seed  seed + 0x9E3779B97F4A7C15 * (i + 1),  so they are the histories an
+ * and clears them, so the graph launches two kernels.  Problem i's
+ * histories use the seed  seed + 0x9E3779B97F4A7C15 * (i + 1),  so they are
+ * the histories an
  * mc_run of that problem alone with that seed would follow.  The problems
  * must outlive the batch and must not be run on their own while a batch run
  * is in flight. */
