@@ -309,8 +309,8 @@ mc_status mc_backward_density(mc_problem *p, const double *params, uint64_t n_hi
  * second kernel in the same graph adds the copies into the problems' sums
  * and clears them, so the graph launches two kernels.  Problem i's
  * histories use the seed  seed + 0x9E3779B97F4A7C15 * (i + 1),  so they are
- * the histories an
- * mc_run of that problem alone with that seed would follow.  The problems
+ * the histories an mc_run of that problem alone with that seed would
+ * follow.  The problems
  * must outlive the batch and must not be run on their own while a batch run
  * is in flight. */
 typedef struct mc_batch mc_batch;
